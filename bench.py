@@ -1,0 +1,369 @@
+"""Benchmark: seconds per IRLBA PCA solve on 1,000,000 cells x 2,000 genes.
+
+One step = one full PCA solve (50 PCs, Krylov subspace 100, tol 1e-6, seed 0)
+of a synthetic negative-binomial count matrix (~5 % density, ~100M stored
+entries, uint16 counts, int32 gene indices, float32 logCP10k size factors)
+with the normalisation fused into the sparse products. The matrix is
+generated on the host from seeded per-chunk streams (identical on every
+machine) and is larger than L2, as are the Lanczos bases.
+
+  value  device-resident solve time (matrix already in HBM) per solve
+  e2e    the same solve through the C ABI with host buffers: host->device copy
+         of the counts, device layout build, solve, device->host copy of the PCs
+  roofline  the kernel class with the most device time, its algorithmic bytes
+         per launch / its CUDA-event time, against the measured HBM copy peak
+  cpu_baseline  the reference's own irlba (compiled from its sources) on this
+         machine's host cores, on a bounded row sample, scaled to a full solve
+
+`--impl reference` times the reference's CPU implementation alone (rank 0).
+Multi-GPU (`--gpus N` under torchrun): N independent replicas, one per GPU;
+the solve itself does not shard ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("s/solve & SpMM HBM GB/s (1M×2000, 50 PCs); batched/served "
+          "solves/s, p99 vs plain")
+UNIT = "s/solve"
+WORKLOADS = {
+    # name: (cells, genes, density, k, m)
+    "plain_1m": (1_000_000, 2000, 0.05, 50, 100),
+    "plain_50k": (50_000, 2000, 0.08, 50, 100),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--cells", type=int, default=0, help="override cell count")
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reorth-passes", type=int, default=2)
+    ap.add_argument("--sample-rows", type=int, default=125_000)
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def workload(args):
+    from brisc_gb300.synth import cached_nb_counts
+    n, g, dens, k, m = WORKLOADS[args.workload]
+    if args.cells:
+        n = args.cells
+    return cached_nb_counts(n, g, seed=0, density=dens), k, m
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                 "-i", str(self.idx), "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = [r.split(", ") for r in Path(self.f.name).read_text().splitlines()
+                if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1].split()[0]))
+                smax.append(float(r[2].split()[0]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def reference_solve_seconds(C, sample_rows: int, k: int, m: int):
+    """One reference irlba solve on the first `sample_rows` cells, scaled to
+    the full cell count. Returns (scaled s/solve, raw seconds, meta) or None."""
+    from oracle import ref
+    mods = ref.load()
+    if mods is None:
+        return None
+    import scipy.sparse as sp
+    ns = min(sample_rows, C.num_cells)
+    ip = C.indptr[: ns + 1].astype(np.int64)
+    nnz = int(ip[-1])
+    ix = C.indices[:nnz].astype(np.int64)
+    data = C.data[:nnz].astype(np.float32)
+    threads = os.cpu_count() or 1
+    xn, _ = ref.normalize(ip, ix, data, 0, threads)
+    csc = sp.csr_matrix((xn, ix, ip), shape=(ns, C.num_genes)).tocsc()
+    csc.sort_indices()
+    csc_t = (csc.indptr.astype(np.int64), csc.indices.astype(np.int64), csc.data)
+    t0 = time.perf_counter()
+    pcs, conv = ref.run_irlba(ip, ix, xn, ns, C.num_genes, k, m, 1e-6, 100, 0,
+                              threads, 1024, csc=csc_t, match_parallel=False)
+    dt = time.perf_counter() - t0
+    return dt * C.num_cells / ns, dt, {"rows": ns, "threads": threads,
+                                       "converged": conv}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init(args)
+    if rank != 0:
+        return 0
+    C, k, m = workload(args)
+    from oracle import ref
+    if ref.load() is None:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "reference modules could not be built on this host"}))
+        return 0
+    times, raws, meta = [], [], None
+    for i in range(args.warmup + args.steps):
+        scaled, raw, meta = reference_solve_seconds(C, args.sample_rows, k, m)
+        if i >= args.warmup:
+            times.append(scaled)
+            raws.append(raw)
+    v = float(np.mean(times))
+    sample = (f"reference irlba (brisc/pca.pyx, -Ofast -fopenmp) full solve on the "
+              f"first {meta['rows']:,} of {C.num_cells:,} cells, "
+              f"{meta['threads']} threads, scaled by cells")
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": float(np.mean(raws)) * 1e3, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic", "impl": "reference",
+           "config": config_of(args, C, k, m),
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": meta["threads"],
+                            "kind": "reference", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def config_of(args, C, k, m):
+    return {"workload": f"{args.workload}: plain IRLBA PCA, {C.num_cells:,} cells x "
+                        f"{C.num_genes:,} genes, NB counts at {C.density:.2%} "
+                        f"density, {k} PCs, subspace {m}, tol 1e-6, logCP10k "
+                        f"fused",
+            "cells": C.num_cells, "genes": C.num_genes, "nnz": C.nnz,
+            "num_PCs": k, "subspace_size": m, "value_dtype": "uint16",
+            "index_dtype": "int32", "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_init(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    torch.cuda.init()
+    from brisc_gb300 import DeviceMatrix
+    C, k, m = workload(args)
+    n, g = C.num_cells, C.num_genes
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # resident matrix (int32 indptr: nnz < 2^31 at this size)
+    ip32 = C.indptr.astype(np.int32)
+    M = DeviceMatrix(ip32, C.indices, C.data, n, g, norm="logCP10k",
+                     inv_size_factors=C.isf, stream=stream)
+    pcs_dev = torch.empty((n, k), dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        r = M.solve(k, m, reorth_passes=args.reorth_passes, PCs=pcs_dev,
+                    stream=stream)
+    barrier()
+    torch.cuda.synchronize()
+    infos = []
+    with Clocks(local) as clk:
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            r = M.solve(k, m, reorth_passes=args.reorth_passes, PCs=pcs_dev,
+                        profile=True, stream=stream)
+            infos.append(r.info)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = start.elapsed_time(stop)
+    clocks = clk.summary()
+    ms_t = torch.tensor([ms], device=dev)
+    launches = torch.tensor([sum(i["kernel_launches"] for i in infos)], device=dev,
+                            dtype=torch.float64)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(launches)
+    ms_max = float(ms_t.item())
+    value = ms_max / 1e3 / (args.steps * ws)
+    last = r
+    M.close()
+
+    # end-to-end through the C ABI with pinned host buffers
+    e2e_steps = args.e2e_steps or min(3, args.steps)
+    h_ip = torch.from_numpy(ip32).pin_memory()
+    h_ix = torch.from_numpy(C.indices).pin_memory()
+    h_v = torch.from_numpy(C.data.view(np.int16)).pin_memory()
+    h_sf = torch.from_numpy(C.isf).pin_memory()
+    h_pcs = torch.empty((n, k), dtype=torch.float32).pin_memory()
+    np_views = [t.numpy() for t in (h_ip, h_ix, h_v, h_sf, h_pcs)]
+    np_views[2] = np_views[2].view(np.uint16)
+    h2d = sum(a.nbytes for a in np_views[:4])
+    d2h = np_views[4].nbytes
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Me = DeviceMatrix(np_views[0], np_views[1], np_views[2], n, g,
+                          norm="logCP10k", inv_size_factors=np_views[3],
+                          stream=stream)
+        Me.solve(k, m, reorth_passes=args.reorth_passes, PCs=np_views[4],
+                 stream=stream)
+        Me.close()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0)
+    e2e_t = torch.tensor([e2e_s], device=dev)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = float(e2e_t.item()) / (e2e_steps * ws)
+
+    if rank != 0:
+        return 0
+    # roofline: the kernel class with the most device time
+    peaks = measured_peaks()
+    tot = lambda key: sum(i[key] for i in infos)  # noqa: E731
+    classes = {
+        "spmv_csr (X.v)": (tot("matvec_seconds"),
+                           infos[0]["matvec_bytes"] * tot("lanczos_steps")),
+        "rmatvec_panels (X^T.u)": (tot("rmatvec_seconds"),
+                                   infos[0]["rmatvec_bytes"] * tot("rmatvecs")),
+        "u_pass (dots/update)": (tot("reorth_seconds"), tot("reorth_bytes")),
+        "restart_rotation": (tot("rotation_seconds"), tot("rotation_bytes")),
+    }
+    dominant = max(classes, key=lambda c: classes[c][0])
+    secs, byts = classes[dominant]
+    achieved = byts / secs / 1e9 if secs > 0 else None
+    sp_secs = tot("matvec_seconds") + tot("rmatvec_seconds")
+    sp_bytes = classes["spmv_csr (X.v)"][1] + classes["rmatvec_panels (X^T.u)"][1]
+    roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved,
+            "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"] if achieved else None,
+            "peak_source": peaks["source"], "traffic": None,
+            "spmm_achieved_gbs": sp_bytes / sp_secs / 1e9 if sp_secs else None,
+            "spmm_frac": (sp_bytes / sp_secs / 1e9 / peaks["hbm_gbs"]) if sp_secs else None,
+            "time_share": {c: classes[c][0] / (ms_max / 1e3) for c in classes}}
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        try:
+            res = reference_solve_seconds(C, args.sample_rows, k, m)
+        except Exception as e:  # noqa: BLE001
+            print(f"[bench] cpu baseline failed: {e}", file=sys.stderr)
+            res = None
+        if res is not None:
+            scaled, raw, meta = res
+            cpu = {"value": scaled, "unit": UNIT, "cores": meta["threads"],
+                   "kind": "reference",
+                   "sample": f"reference irlba full solve on the first "
+                             f"{meta['rows']:,} cells ({raw:.2f} s), scaled by "
+                             f"cells to {n:,}"}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms_max / args.steps, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic", "config": config_of(args, C, k, m),
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+           "gpu_launches": int(launches.item()),
+           "solve": {"restarts": last.info["restarts"],
+                     "lanczos_steps": last.info["lanczos_steps"],
+                     "converged": last.converged,
+                     "seconds_host": last.info["seconds"]}}
+    print(json.dumps(out))
+    return 0
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,360 @@
+// Dense kernels of the IRLBA solve: the fused U pass of brisc/pca.pyx:997-1090
+// split into fixed-block dot / update kernels (classical Gram-Schmidt, run
+// once as the reference or twice for CGS2), the V-side step of pca.pyx:1103-1171
+// and the tall-skinny rotations of pca.pyx:1210-1255.
+//
+// Determinism: every sum is either a per-thread sequence in a fixed order, a
+// fixed xor-shuffle tree, or a sum over fixed 1024-row blocks in block order.
+#include <algorithm>
+
+#include "dense.cuh"
+
+namespace bgpu {
+
+namespace {
+
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+}
+
+__global__ void __launch_bounds__(256)
+k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+        const float* __restrict__ y, float* __restrict__ part,
+        uint32_t pstride, int with_sum) {
+  __shared__ float red[8][9];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t b = blockIdx.x;
+  const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
+  const bool in = row0 < ldu;
+  const float4 yv = in ? *reinterpret_cast<const float4*>(y + row0)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (with_sum) {
+    float s = warp_sum(yv.x + yv.y + yv.z + yv.w);
+    if (lane == 0) red[wid][8] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w][8];
+      part[b * pstride + ncols] = t;
+    }
+  }
+  for (uint32_t c0 = 0; c0 < ncols; c0 += 8) {
+    float acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t c = c0 + k;
+      acc[k] = 0.f;
+      if (in && c < ncols) {
+        const float4 u = __ldcs(reinterpret_cast<const float4*>(U + c * ldu + row0));
+        acc[k] = dot4(u, yv);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) red[wid][k] = acc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && c0 + threadIdx.x < ncols) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w][threadIdx.x];
+      part[b * pstride + c0 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+          const float* __restrict__ coef, const float* __restrict__ mean_sum,
+          uint64_t n, const float* __restrict__ y_in, float* __restrict__ y_out,
+          float* __restrict__ norm_part, uint32_t pstride) {
+  extern __shared__ float cs[];
+  __shared__ float red[8];
+  for (uint32_t c = threadIdx.x; c < ncols; c += blockDim.x) cs[c] = coef[c];
+  __syncthreads();
+  const uint64_t b = blockIdx.x;
+  const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
+  float sq = 0.f;
+  if (row0 < ldu) {
+    float4 yv = *reinterpret_cast<const float4*>(y_in + row0);
+    const float mean = mean_sum ? (*mean_sum) / (float)n : 0.f;  // pca.pyx:1025-1028
+    float4 t = make_float4(mean, mean, mean, mean);
+#pragma unroll 8
+    for (uint32_t c = 0; c < ncols; ++c) {
+      const float4 u = __ldcs(reinterpret_cast<const float4*>(U + c * ldu + row0));
+      const float w = cs[c];
+      t.x += u.x * w;
+      t.y += u.y * w;
+      t.z += u.z * w;
+      t.w += u.w * w;
+    }
+    yv.x = (row0 + 0 < n) ? yv.x - t.x : 0.f;
+    yv.y = (row0 + 1 < n) ? yv.y - t.y : 0.f;
+    yv.z = (row0 + 2 < n) ? yv.z - t.z : 0.f;
+    yv.w = (row0 + 3 < n) ? yv.w - t.w : 0.f;
+    *reinterpret_cast<float4*>(y_out + row0) = yv;
+    sq = yv.x * yv.x + yv.y * yv.y + yv.z * yv.z + yv.w * yv.w;
+  }
+  if (norm_part) {
+    sq = warp_sum(sq);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sq;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w];
+      norm_part[b * pstride] = t;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
+              uint32_t ncols, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (c >= ncols) return;
+  float t = 0.f;
+  for (uint64_t b = lane; b < nblocks; b += 32) t += part[b * pstride + c];
+  t = warp_sum(t);
+  if (lane == 0) out[c] = t;
+}
+
+__global__ void __launch_bounds__(256)
+k_finish_norm(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
+              double* __restrict__ B, uint32_t m, uint32_t j,
+              float* __restrict__ scal) {
+  __shared__ double red[8];
+  double t = 0.0;
+  for (uint64_t b = threadIdx.x; b < nblocks; b += blockDim.x)
+    t += (double)part[b * pstride];
+  t = warp_sum(t);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += red[w];
+    double a = sqrt(s);
+    if (a < 1e-8) a = 1e-8;  // clip_val, pca.pyx:1084-1085
+    B[j + (uint64_t)j * m] = a;
+    const float af = (float)a;
+    scal[0] = af;
+    scal[1] = 1.f / af;  // inverse_alpha, pca.pyx:1086
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+k_vstep(const float* __restrict__ zpart, uint32_t num_panels,
+        const float* __restrict__ sd, float* __restrict__ V, uint64_t ldv,
+        uint32_t g, uint32_t j, uint32_t m, const float* __restrict__ scal,
+        double* __restrict__ B, float* __restrict__ rem, int passes) {
+  extern __shared__ float dots[];  // m floats
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const float alpha = scal[0];
+  float* z = (j + 1 < m) ? V + (uint64_t)(j + 1) * ldv : rem;
+  const float* vj = V + (uint64_t)j * ldv;
+  for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) {
+    float t = 0.f;
+    for (uint32_t p = 0; p < num_panels; ++p) t += zpart[(uint64_t)p * g + c];
+    t = t / sd[c];           // pca.pyx:510-511
+    z[c] = t - alpha * vj[c];  // pca.pyx:1104-1105
+  }
+  __syncthreads();
+  for (int pass = 0; pass < passes; ++pass) {
+    for (uint32_t col = wid; col <= j; col += 32) {
+      const float* vc = V + (uint64_t)col * ldv;
+      float d = 0.f;
+      for (uint32_t c = lane; c < g; c += 32) d += vc[c] * z[c];
+      d = warp_sum(d);
+      if (lane == 0) dots[col] = d;
+    }
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) {
+      float t = 0.f;
+      for (uint32_t col = 0; col <= j; ++col) t += V[c + (uint64_t)col * ldv] * dots[col];
+      z[c] -= t;
+    }
+    __syncthreads();
+  }
+  if (j + 1 < m) {
+    double ss = 0.0;
+    for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) ss += (double)z[c] * z[c];
+    ss = warp_sum(ss);
+    if (lane == 0) red[wid] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < 32; ++w) s += red[w];
+      double beta = sqrt(s);
+      if (beta < 1e-8) beta = 1e-8;  // pca.pyx:1165-1166
+      B[j + (uint64_t)(j + 1) * m] = beta;
+      red[0] = beta;
+    }
+    __syncthreads();
+    const float inv = 1.f / (float)red[0];
+    for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) z[c] *= inv;
+  }
+}
+
+// Tall-skinny SIMT GEMM: CTA tile 128 rows x 128 columns, K in steps of 16.
+constexpr int BM = 128, BN = 128, BK = 16;
+
+__global__ void __launch_bounds__(256)
+k_gemm_ts(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
+          const float* __restrict__ Bp, uint64_t bsr, uint64_t bsc,
+          const float* __restrict__ cs, uint32_t ncols, float* __restrict__ C,
+          uint64_t ldc, int c_rowmajor) {
+  __shared__ __align__(16) float As[BK][BM];
+  __shared__ __align__(16) float Bs[BK][BN];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const uint64_t r0 = (uint64_t)blockIdx.x * BM;
+  const uint32_t c0 = blockIdx.y * BN;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) acc[i][jj] = 0.f;
+
+  for (uint32_t k0 = 0; k0 < K; k0 += BK) {
+    // A tile: 16 columns x 128 rows; thread loads 8 floats (2 x float4)
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int idx = tid + t * 256;       // 0..511 float4 slots
+      const int kk = idx >> 5;             // 0..15
+      const int rr = (idx & 31) * 4;       // 0..124
+      const uint64_t r = r0 + rr;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k0 + kk < K) {
+        const float* src = A + (uint64_t)(k0 + kk) * lda + r;
+        if (r + 3 < rows) {
+          v = *reinterpret_cast<const float4*>(src);
+        } else {
+          if (r + 0 < rows) v.x = src[0];
+          if (r + 1 < rows) v.y = src[1];
+          if (r + 2 < rows) v.z = src[2];
+        }
+      }
+      *reinterpret_cast<float4*>(&As[kk][rr]) = v;
+    }
+    // B tile: 16 x 128, strided gather (small operand, L2-resident)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int idx = tid + t * 256;  // 0..2047
+      const int kk = idx >> 7;
+      const int cc = idx & 127;
+      float v = 0.f;
+      if (k0 + kk < K && c0 + cc < ncols) {
+        v = Bp[(uint64_t)(k0 + kk) * bsr + (uint64_t)(c0 + cc) * bsc];
+        if (cs) v *= cs[c0 + cc];
+      }
+      Bs[kk][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) acc[i][jj] += a[i] * bb[jj];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint64_t r = r0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+    if (r >= rows) continue;
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      const uint32_t c = c0 + (jj < 4 ? tx * 4 + jj : 64 + tx * 4 + (jj - 4));
+      if (c >= ncols) continue;
+      if (c_rowmajor)
+        C[r * ldc + c] = acc[i][jj];
+      else
+        C[r + (uint64_t)c * ldc] = acc[i][jj];
+    }
+  }
+}
+
+__global__ void k_b_to_float(const double* __restrict__ B, uint64_t count,
+                             float* __restrict__ Bf) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < count) Bf[i] = (float)B[i];
+}
+
+}  // namespace
+
+int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
+                 uint64_t nblocks, float* part, uint32_t pstride, bool with_sum,
+                 cudaStream_t s) {
+  k_udots<<<(unsigned)nblocks, 256, 0, s>>>(U, ldu, ncols, y, part, pstride,
+                                            with_sum ? 1 : 0);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
+                   const float* coef, const float* mean_sum, uint64_t n,
+                   const float* y_in, float* y_out, uint64_t nblocks,
+                   float* norm_part, uint32_t pstride, cudaStream_t s) {
+  k_uupdate<<<(unsigned)nblocks, 256, std::max<size_t>(ncols, 1) * 4, s>>>(
+      U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
+                       uint32_t ncols, float* out, cudaStream_t s) {
+  if (ncols == 0) return BGPU_OK;
+  k_reduce_cols<<<(unsigned)ceil_div(ncols, 8), 256, 0, s>>>(part, nblocks,
+                                                             pstride, ncols, out);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
+                       double* B, uint32_t m, uint32_t j, float* scal,
+                       cudaStream_t s) {
+  k_finish_norm<<<1, 256, 0, s>>>(part, nblocks, pstride, B, m, j, scal);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_vstep(const float* zpart, uint32_t num_panels, const float* sd,
+                 float* V, uint64_t ldv, uint32_t g, uint32_t j, uint32_t m,
+                 const float* scal, double* B, float* rem, int passes,
+                 cudaStream_t s) {
+  k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(
+      zpart, num_panels, sd, V, ldv, g, j, m, scal, B, rem, passes);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_gemm_ts(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                   const float* Bp, uint64_t bsr, uint64_t bsc, const float* cs,
+                   uint32_t ncols, float* C, uint64_t ldc, bool c_rowmajor,
+                   cudaStream_t s) {
+  if (rows == 0 || ncols == 0) return BGPU_OK;
+  dim3 grid((unsigned)ceil_div(rows, BM), (unsigned)ceil_div(ncols, BN));
+  k_gemm_ts<<<grid, 256, 0, s>>>(A, lda, rows, K, Bp, bsr, bsc, cs, ncols, C,
+                                 ldc, c_rowmajor ? 1 : 0);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_b_to_float(const double* B, uint32_t m, float* Bf, cudaStream_t s) {
+  uint64_t count = (uint64_t)m * (m + 1);
+  k_b_to_float<<<(unsigned)ceil_div(count, 256), 256, 0, s>>>(B, count, Bf);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+}  // namespace bgpu

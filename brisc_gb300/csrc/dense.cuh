@@ -1,0 +1,55 @@
+// Dense kernels of the IRLBA solve (internal).
+#pragma once
+
+#include "common.cuh"
+
+namespace bgpu {
+
+constexpr int kRowBlock = 1024;  // rows per fixed reduction block (256 threads x 4)
+
+// part[b * pstride + c] = U[rows of b, c] . y[rows of b]   for c < ncols
+// and, when with_sum, part[b * pstride + ncols] = sum(y[rows of b]).
+int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
+                 uint64_t nblocks, float* part, uint32_t pstride, bool with_sum,
+                 cudaStream_t s);
+
+// y_out = y_in - (mean + U[:, :ncols] . coef)   for rows < n, 0 beyond.
+// mean = (*mean_sum) / n when mean_sum is non-null (the reference's
+// `dot_product = mean; dot_product += U[row, col] * work[col]`, pca.pyx:1045).
+// When norm_part is non-null, norm_part[b * pstride] = sum(y_out^2) per block.
+int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
+                   const float* coef, const float* mean_sum, uint64_t n,
+                   const float* y_in, float* y_out, uint64_t nblocks,
+                   float* norm_part, uint32_t pstride, cudaStream_t s);
+
+// out[c] = sum_b part[b * pstride + c] in block order (one warp per column).
+int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
+                       uint32_t ncols, float* out, cudaStream_t s);
+
+// alpha = max(sqrt(sum_b part[b*pstride]), 1e-8) (FP64 sum); B[j,j] = alpha;
+// writes alpha (float) and 1/alpha (float) to scal[0], scal[1].
+int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
+                       double* B, uint32_t m, uint32_t j, float* scal,
+                       cudaStream_t s);
+
+// V-side half step (pca.pyx:1103-1171): z = (sum_p zpart[p]) / sd - alpha V[:, j],
+// `passes` rounds of classical Gram-Schmidt against V[:, :j+1]; then either
+// V[:, j+1] = z / beta, B[j, j+1] = beta (j < m-1) or rem = z (j == m-1).
+int launch_vstep(const float* zpart, uint32_t num_panels, const float* sd,
+                 float* V, uint64_t ldv, uint32_t g, uint32_t j, uint32_t m,
+                 const float* scal, double* B, float* rem, int passes,
+                 cudaStream_t s);
+
+// C = A . Bop (tall-skinny): A is rows x K column-major (lda), Bop(i, c) =
+// Bp[i * bsr + c * bsc] (K x ncols), optional per-column scale cs[c] applied
+// to Bop. Output column-major (ldc) or, when c_rowmajor, row-major with row
+// stride ldc. Each output is one fixed-order dot product (deterministic).
+int launch_gemm_ts(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                   const float* Bp, uint64_t bsr, uint64_t bsc,
+                   const float* cs, uint32_t ncols, float* C, uint64_t ldc,
+                   bool c_rowmajor, cudaStream_t s);
+
+// B (m x (m+1), column-major FP64) -> float copy for the small SVD.
+int launch_b_to_float(const double* B, uint32_t m, float* Bf, cudaStream_t s);
+
+}  // namespace bgpu

@@ -1,0 +1,609 @@
+// IRLBA driver (host C++) and the C-ABI entry points.
+//
+// The restart loop follows brisc/pca.pyx:982-1231 (the deterministic parallel
+// path): for every restart, Lanczos steps j = k_current .. m-1 (X.v, fused U
+// pass, X^T.u, V-side step), then the small SVD of B, the convergence test and
+// the restart rotation. All vector work stays on the GPU; the host only reads
+// a 32-byte restart status per restart (to learn k_current and convergence).
+//
+// Deviation kept on purpose: when max_iterations is reached
+// without convergence, the reference rotates U once more and then multiplies
+// by Ub again (pca.pyx:1210-1215 then 1253), mixing in stale buffer columns;
+// here the last restart is not rotated, so the returned PCs are the Ritz
+// vectors of the final SVD, scaled by their singular values.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dense.cuh"
+#include "matrix.cuh"
+#include "svd.cuh"
+
+namespace bgpu {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* get_error() { return g_last_error.c_str(); }
+
+int num_sms() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return kNumSMs;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (!cache[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = kNumSMs;
+    cache[dev] = v;
+  }
+  return cache[dev];
+}
+
+// ---------------------------------------------------------------------------
+// PCG32 + Box-Muller start vector, restating brisc/cyutils.pyx:1153-1232 and
+// brisc/pca.pyx:801-806 operation for operation (float arithmetic as there).
+namespace {
+
+inline uint32_t pcg_rand(uint64_t* state) {  // cyutils.pyx:1153-1158
+  const uint64_t x = *state;
+  *state = x * 6364136223846793005ULL + 1442695040888963407ULL;
+  const uint32_t s = (uint32_t)((x ^ (x >> 18)) >> 27);
+  const uint32_t rot = (uint32_t)(x >> 59);
+  return (s >> rot) | (s << ((0u - rot) & 31u));
+}
+
+inline uint64_t pcg_srand(uint64_t seed) {  // cyutils.pyx:1228-1232
+  uint64_t state = seed + 1442695040888963407ULL;
+  pcg_rand(&state);
+  return state;
+}
+
+inline float pcg_uniform(uint64_t* state) {  // cyutils.pyx:1175-1177
+  return (float)pcg_rand(state) / (float)4294967295u;
+}
+
+inline float pcg_normal(uint64_t* state) {  // cyutils.pyx:1180-1191
+  float u1;
+  while (true) {
+    u1 = pcg_uniform(state);
+    if (u1 != 0) break;
+  }
+  const float u2 = pcg_uniform(state);
+  const float r = std::sqrt(-2 * std::log(u1));
+  const float theta = (float)(2 * 3.14159265358979323846 * (double)u2);
+  return r * std::cos(theta);
+}
+
+}  // namespace
+
+int start_vector(uint64_t seed, uint32_t g, float* out) {
+  uint64_t state = pcg_srand(seed);
+  for (uint32_t i = 0; i < g; ++i) out[i] = pcg_normal(&state);
+  float nrm = 0;  // cyutils.pyx:1089-1094
+  for (uint32_t i = 0; i < g; ++i) nrm += out[i] * out[i];
+  nrm = std::sqrt(nrm);
+  const float inv = 1 / nrm;
+  for (uint32_t i = 0; i < g; ++i) out[i] *= inv;
+  return BGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Buf {
+  void* p = nullptr;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  ~Buf() { if (p) cudaFree(p); }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+int balloc(Buf& b, size_t bytes, bool zero, cudaStream_t s) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    set_error(std::string("cudaMalloc(") + std::to_string(bytes) +
+              ") failed: " + cudaGetErrorString(e));
+    return BGPU_ERR_ALLOC;
+  }
+  if (zero) BGPU_CUDA(cudaMemsetAsync(b.p, 0, bytes, s));
+  return BGPU_OK;
+}
+
+struct PinnedStatus {
+  RestartStatus* h = nullptr;
+  ~PinnedStatus() { if (h) cudaFreeHost(h); }
+};
+
+struct Solver {
+  const Matrix& X;
+  uint64_t n;
+  uint32_t g, k, m;
+  uint64_t ldu, ldv, nb;
+  uint32_t ps;
+  int passes;
+  cudaStream_t s;
+  float tol;
+
+  Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, rem, sd, Bf, Ub, Sb, Vbt,
+      svdwork, scal, smax, B, st, sdpart, svdinfo;
+  PinnedStatus hst;
+
+  // accounting
+  uint64_t launches = 0;
+  double reorth_bytes = 0, rotation_bytes = 0;
+  // profiling: event pairs around the sparse products and the small SVD
+  bool profile = false;
+  std::vector<cudaEvent_t> ev;
+  // kinds: 0 X.v, 1 X^T.u, 2 SVD, 3 U pass, 4 V step, 5 rotation
+  std::vector<int> ev_kind;
+  size_t ev_used = 0;
+  double t_kind[6] = {0, 0, 0, 0, 0, 0};
+
+  ~Solver() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+
+  int ev_begin(int kind) {
+    if (!profile) return BGPU_OK;
+    if (ev_used + 2 > ev.size()) {
+      for (int i = 0; i < 2; ++i) {
+        cudaEvent_t e;
+        BGPU_CUDA(cudaEventCreate(&e));
+        ev.push_back(e);
+      }
+      ev_kind.push_back(0);
+    }
+    ev_kind[ev_used / 2] = kind;
+    BGPU_CUDA(cudaEventRecord(ev[ev_used], s));
+    return BGPU_OK;
+  }
+  int ev_end() {
+    if (!profile) return BGPU_OK;
+    BGPU_CUDA(cudaEventRecord(ev[ev_used + 1], s));
+    ev_used += 2;
+    return BGPU_OK;
+  }
+  // Called after the stream has been synchronised.
+  int ev_collect() {
+    for (size_t i = 0; i < ev_used; i += 2) {
+      float ms = 0.f;
+      BGPU_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+      t_kind[ev_kind[i / 2]] += ms * 1e-3;
+    }
+    ev_used = 0;
+    return BGPU_OK;
+  }
+
+  Solver(const Matrix& X_, const bgpu_solve_opts& o, cudaStream_t s_)
+      : X(X_), n(X_.n), g(X_.g), k(o.k), m(o.subspace_size), s(s_),
+        tol(o.tolerance) {
+    ldu = basis_ld(n);
+    ldv = basis_ld(g);
+    nb = ceil_div(n, kRowBlock);
+    ps = m + 2;
+    passes = o.reorth_passes == 1 ? 1 : 2;
+  }
+
+  int alloc() {
+    BGPU_TRY(balloc(U, ldu * m * 4, true, s));
+    BGPU_TRY(balloc(Unew, ldu * m * 4, true, s));
+    BGPU_TRY(balloc(V, ldv * m * 4, true, s));
+    BGPU_TRY(balloc(Vnew, ldv * m * 4, true, s));
+    BGPU_TRY(balloc(y0, ldu * 4, true, s));
+    BGPU_TRY(balloc(y1, ldu * 4, true, s));
+    BGPU_TRY(balloc(part, nb * ps * 4, true, s));
+    BGPU_TRY(balloc(coef, 2 * (size_t)ps * 4, true, s));
+    BGPU_TRY(balloc(zpart, (size_t)X.num_panels * g * 4, true, s));
+    BGPU_TRY(balloc(rem, ldv * 4, true, s));
+    BGPU_TRY(balloc(sd, ldv * 4, true, s));
+    BGPU_TRY(balloc(Bf, (size_t)m * (m + 1) * 4, true, s));
+    BGPU_TRY(balloc(Ub, (size_t)m * m * 4, true, s));
+    BGPU_TRY(balloc(Sb, (size_t)m * 4, true, s));
+    BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
+    if (jacobi_smem_bytes(m) > 220 * 1024)
+      BGPU_TRY(balloc(svdwork, jacobi_global_floats(m) * 4, true, s));
+    BGPU_TRY(balloc(scal, 64, true, s));
+    BGPU_TRY(balloc(smax, 64, false, s));
+    BGPU_TRY(balloc(B, (size_t)m * (m + 1) * 8, true, s));
+    BGPU_TRY(balloc(st, sizeof(RestartStatus), true, s));
+    BGPU_TRY(balloc(sdpart, (size_t)X.num_panels * g * 16, false, s));
+    BGPU_TRY(balloc(svdinfo, 16, true, s));
+    BGPU_CUDA(cudaMallocHost((void**)&hst.h, sizeof(RestartStatus)));
+    return BGPU_OK;
+  }
+
+  float* Ucol(uint32_t j) const { return U.as<float>() + (uint64_t)j * ldu; }
+  float* Vcol(uint32_t j) const { return V.as<float>() + (uint64_t)j * ldv; }
+
+  int step(uint32_t j) {
+    float* y0p = y0.as<float>();
+    float* y1p = y1.as<float>();
+    float* partp = part.as<float>();
+    float* coefp = coef.as<float>();
+    float* coef2 = coefp + ps;
+    float* Up = U.as<float>();
+    BGPU_TRY(ev_begin(0));
+    BGPU_TRY(launch_matvec(X, Vcol(j), sd.as<float>(), y0p, s));
+    BGPU_TRY(ev_end());
+    launches += 1;
+    const double col = (double)n * 4.0;
+    BGPU_TRY(ev_begin(3));
+    float* yfin;
+    if (j == 0) {
+      BGPU_TRY(launch_udots(Up, ldu, 0, y0p, nb, partp, ps, true, s));
+      BGPU_TRY(launch_reduce_cols(partp, nb, ps, 1, coefp, s));
+      BGPU_TRY(launch_uupdate(Up, ldu, 0, coefp, coefp, n, y0p, y1p, nb, partp,
+                              ps, s));
+      launches += 3;
+      reorth_bytes += 3 * col;
+      yfin = y1p;
+    } else {
+      BGPU_TRY(launch_udots(Up, ldu, j, y0p, nb, partp, ps, true, s));
+      BGPU_TRY(launch_reduce_cols(partp, nb, ps, j + 1, coefp, s));
+      launches += 2;
+      reorth_bytes += (j + 1) * col;
+      if (passes == 1) {
+        BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
+                                partp, ps, s));
+        launches += 1;
+        reorth_bytes += (j + 2) * col;
+        yfin = y1p;
+      } else {
+        BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
+                                nullptr, ps, s));
+        BGPU_TRY(launch_udots(Up, ldu, j, y1p, nb, partp, ps, false, s));
+        BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s));
+        BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y1p, y0p, nb,
+                                partp, ps, s));
+        launches += 4;
+        reorth_bytes += ((j + 2) + (j + 1) + (j + 2)) * col;
+        yfin = y0p;
+      }
+    }
+    float* scalp = scal.as<float>();
+    BGPU_TRY(launch_finish_norm(partp, nb, ps, B.as<double>(), m, j, scalp, s));
+    BGPU_TRY(ev_end());
+    BGPU_TRY(ev_begin(1));
+    BGPU_TRY(launch_rmatvec_partials(X, yfin, scalp + 1, Ucol(j),
+                                     zpart.as<float>(), s));
+    BGPU_TRY(ev_end());
+    BGPU_TRY(ev_begin(4));
+    BGPU_TRY(launch_vstep(zpart.as<float>(), X.num_panels, sd.as<float>(),
+                          V.as<float>(), ldv, g, j, m, scalp, B.as<double>(),
+                          rem.as<float>(), passes, s));
+    BGPU_TRY(ev_end());
+    launches += 3;
+    reorth_bytes += (double)(j + 1) * g * 4.0 * 2 * passes;
+    return BGPU_OK;
+  }
+};
+
+}  // namespace
+
+int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
+                int pcs_on_device, float* svals, float* loadings,
+                bgpu_solve_info* info, cudaStream_t s) {
+  const auto t0 = std::chrono::steady_clock::now();
+  BGPU_REQUIRE(o.k >= 1, BGPU_ERR_INVALID, "num_PCs (k) must be >= 1");
+  BGPU_REQUIRE(o.subspace_size >= o.k, BGPU_ERR_INVALID,
+               "subspace_size must be >= num_PCs");
+  BGPU_REQUIRE(X.n >= 2 && X.g >= 2, BGPU_ERR_INVALID,
+               "PCA needs at least two cells and two genes");
+  BGPU_REQUIRE((uint64_t)o.subspace_size <= std::min<uint64_t>(X.n, X.g),
+               BGPU_ERR_INVALID,
+               "subspace_size must be <= min(num_cells, num_genes)");
+  BGPU_REQUIRE(o.subspace_size <= 1024, BGPU_ERR_UNSUPPORTED,
+               "subspace_size must be <= 1024");
+  BGPU_REQUIRE(o.max_iterations >= 1, BGPU_ERR_INVALID,
+               "max_iterations must be >= 1");
+  BGPU_REQUIRE(o.tolerance > 0.f, BGPU_ERR_INVALID, "tolerance must be > 0");
+  BGPU_REQUIRE(pcs != nullptr, BGPU_ERR_INVALID, "PCs must not be NULL");
+
+  Solver S(X, o, s);
+  S.profile = o.profile != 0;
+  BGPU_TRY(S.alloc());
+  const uint32_t m = S.m, k = S.k, g = S.g;
+
+  // Gene scaling (pca.pyx:790-799) and start vector (pca.pyx:801-806).
+  BGPU_TRY(launch_gene_stddev(X, S.sdpart.as<double>(), S.sd.as<float>(), s));
+  S.launches += 2;
+  {
+    std::vector<float> v0(g);
+    start_vector(o.seed, g, v0.data());
+    BGPU_CUDA(cudaMemcpyAsync(S.Vcol(0), v0.data(), g * 4, cudaMemcpyHostToDevice, s));
+    const float smax0 = 2.4221817809573368e-05f;  // pca.pyx:688
+    BGPU_CUDA(cudaMemcpyAsync(S.smax.p, &smax0, 4, cudaMemcpyHostToDevice, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));  // v0, smax0 are host stack values
+  }
+
+  uint32_t kc = 0, restarts = 0, steps = 0;
+  RestartStatus last{};
+  bool converged = false;
+  for (uint32_t it = 0; it < o.max_iterations; ++it) {
+    for (uint32_t j = kc; j < m; ++j) {
+      if (o.cancel && *o.cancel) {
+        cudaStreamSynchronize(s);
+        set_error("solve cancelled");
+        return BGPU_ERR_CANCELLED;
+      }
+      BGPU_TRY(S.step(j));
+      ++steps;
+    }
+    ++restarts;
+    BGPU_TRY(launch_b_to_float(S.B.as<double>(), m, S.Bf.as<float>(), s));
+    BGPU_TRY(S.ev_begin(2));
+    BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), m, S.Ub.as<float>(),
+                               S.Sb.as<float>(), S.Vbt.as<float>(),
+                               S.svdwork.as<float>(), S.svdinfo.as<int>(), s));
+    BGPU_TRY(S.ev_end());
+    S.launches += 3;
+    BGPU_TRY(launch_restart_check(S.Ub.as<float>(), S.Sb.as<float>(), m, k,
+                                  S.rem.as<float>(), g, o.tolerance,
+                                  S.smax.as<float>(), kc, S.B.as<double>(),
+                                  S.st.as<RestartStatus>(), s));
+    BGPU_CUDA(cudaMemcpyAsync(S.hst.h, S.st.p, sizeof(RestartStatus),
+                              cudaMemcpyDeviceToHost, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));
+    BGPU_TRY(S.ev_collect());
+    last = *S.hst.h;
+    if (last.converged) { converged = true; break; }
+    if (it + 1 == o.max_iterations) break;
+    kc = (uint32_t)last.k_current;
+    // Restart rotation (pca.pyx:1210-1226): U <- U Ub[:, :kc], V <- V Vbt^T.
+    BGPU_TRY(S.ev_begin(5));
+    BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1,
+                            m, nullptr, kc, S.Unew.as<float>(), S.ldu, false, s));
+    BGPU_TRY(launch_gemm_ts(S.V.as<float>(), S.ldv, g, m, S.Vbt.as<float>(), m,
+                            1, nullptr, kc, S.Vnew.as<float>(), S.ldv, false, s));
+    BGPU_CUDA(cudaMemcpyAsync(S.Vnew.as<float>() + (uint64_t)kc * S.ldv,
+                              S.rem.p, g * 4, cudaMemcpyDeviceToDevice, s));
+    BGPU_TRY(S.ev_end());
+    std::swap(S.U.p, S.Unew.p);
+    std::swap(S.V.p, S.Vnew.p);
+    S.launches += 2;
+    S.rotation_bytes += ((double)S.n + g) * ((double)m + kc) * 4.0;
+  }
+
+  // Final PCs (pca.pyx:1239-1255): PCs = U . (Ub[:, :k] * Sb[:k]), C order.
+  Buf pdev;
+  float* pout = pcs;
+  if (!pcs_on_device) {
+    BGPU_TRY(balloc(pdev, S.n * k * 4, false, s));
+    pout = pdev.as<float>();
+  }
+  BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1, m,
+                          S.Sb.as<float>(), k, pout, k, true, s));
+  if (!pcs_on_device)
+    BGPU_CUDA(cudaMemcpyAsync(pcs, pout, S.n * k * 4, cudaMemcpyDeviceToHost, s));
+  if (svals)
+    BGPU_CUDA(cudaMemcpyAsync(svals, S.Sb.p, k * 4, cudaMemcpyDeviceToHost, s));
+  Buf ldev;
+  if (loadings) {
+    BGPU_TRY(balloc(ldev, (size_t)g * k * 4, false, s));
+    BGPU_TRY(launch_gemm_ts(S.V.as<float>(), S.ldv, g, m, S.Vbt.as<float>(), m, 1,
+                            nullptr, k, ldev.as<float>(), k, true, s));
+    BGPU_CUDA(cudaMemcpyAsync(loadings, ldev.p, (size_t)g * k * 4,
+                              cudaMemcpyDeviceToHost, s));
+  }
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  if (info) {
+    info->converged = converged ? 1 : 0;
+    info->restarts = restarts;
+    info->lanczos_steps = steps;
+    info->rmatvecs = steps;
+    info->num_converged = (uint32_t)last.num_converged;
+    info->k_current = (uint32_t)last.k_current;
+    info->seconds = std::chrono::duration<double>(
+                        std::chrono::steady_clock::now() - t0).count();
+    info->matvec_seconds = S.t_kind[0];
+    info->rmatvec_seconds = S.t_kind[1];
+    info->svd_seconds = S.t_kind[2];
+    info->reorth_seconds = S.t_kind[3];
+    info->vstep_seconds = S.t_kind[4];
+    info->rotation_seconds = S.t_kind[5];
+    info->matvec_bytes = matvec_bytes(X);
+    info->rmatvec_bytes = rmatvec_bytes(X);
+    info->reorth_bytes = S.reorth_bytes;
+    info->rotation_bytes = S.rotation_bytes;
+    info->kernel_launches = S.launches + 1 + (loadings ? 1 : 0);
+  }
+  return BGPU_OK;
+}
+
+}  // namespace bgpu
+
+// ===========================================================================
+// C ABI
+using namespace bgpu;
+
+struct bgpu_matrix {
+  Matrix m;
+};
+
+extern "C" const char* bgpu_last_error(void) { return get_error(); }
+
+extern "C" const char* bgpu_version(void) { return "brisc_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" void bgpu_solve_opts_default(bgpu_solve_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->k = 50;
+  o->subspace_size = 100;
+  o->tolerance = 1e-6f;
+  o->max_iterations = 100;
+  o->seed = 0;
+  o->chunk_size = 1024;
+  o->reorth_passes = 2;
+  o->rotation_mode = 0;
+  o->cancel = nullptr;
+  o->use_graphs = 0;
+}
+
+static void choose_shapes(Matrix& m) {
+  const double avg = m.n ? (double)m.nnz / (double)m.n : 0.0;
+  int G = 4;
+  while (G < 32 && G * 8 < avg) G *= 2;  // about two 4-entry loads per lane
+  m.spmv_group = G;
+  m.spmv_blocks = num_sms() * 8;
+  m.rmat_colgroup = m.g <= 512 ? 64 : 256;
+}
+
+extern "C" int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* d,
+                                  void* stream) {
+  BGPU_REQUIRE(out != nullptr, BGPU_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  bgpu_matrix* h = new (std::nothrow) bgpu_matrix();
+  BGPU_REQUIRE(h != nullptr, BGPU_ERR_ALLOC, "host allocation failed");
+  int rc = matrix_build(&h->m, d, (cudaStream_t)stream);
+  if (rc != BGPU_OK) {
+    matrix_free(&h->m);
+    delete h;
+    return rc;
+  }
+  choose_shapes(h->m);
+  *out = h;
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_matrix_destroy(bgpu_matrix* mat) {
+  if (!mat) return BGPU_OK;
+  matrix_free(&mat->m);
+  delete mat;
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes) {
+  BGPU_REQUIRE(mat && bytes, BGPU_ERR_INVALID, "NULL argument");
+  *bytes = mat->m.bytes;
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_matrix_matvec(const bgpu_matrix* mat, const float* v,
+                                  const float* sd, float* y, void* stream) {
+  BGPU_REQUIRE(mat && v && y, BGPU_ERR_INVALID, "NULL argument");
+  return launch_matvec(mat->m, v, sd, y, (cudaStream_t)stream);
+}
+
+extern "C" int bgpu_matrix_rmatvec(const bgpu_matrix* mat, const float* u,
+                                   const float* sd, float* z, void* stream) {
+  BGPU_REQUIRE(mat && u && z, BGPU_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf part;
+  BGPU_TRY(balloc(part, (size_t)mat->m.num_panels * mat->m.g * 4, false, s));
+  BGPU_TRY(launch_rmatvec_partials(mat->m, u, nullptr, nullptr, part.as<float>(), s));
+  BGPU_TRY(launch_reduce_panels(mat->m, part.as<float>(), sd, z, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_matrix_gene_stddev(const bgpu_matrix* mat, float* sd,
+                                       void* stream) {
+  BGPU_REQUIRE(mat && sd, BGPU_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf part;
+  BGPU_TRY(balloc(part, (size_t)mat->m.num_panels * mat->m.g * 16, false, s));
+  BGPU_TRY(launch_gene_stddev(mat->m, part.as<double>(), sd, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
+                          float* pcs, int pcs_on_device, float* singular_values,
+                          float* loadings, bgpu_solve_info* info, void* stream) {
+  BGPU_REQUIRE(mat && opts, BGPU_ERR_INVALID, "NULL argument");
+  return irlba_solve(mat->m, *opts, pcs, pcs_on_device, singular_values,
+                     loadings, info, (cudaStream_t)stream);
+}
+
+extern "C" int bgpu_start_vector(uint64_t seed, uint32_t num_genes,
+                                 float* out_host) {
+  BGPU_REQUIRE(out_host && num_genes >= 1, BGPU_ERR_INVALID, "bad arguments");
+  return start_vector(seed, num_genes, out_host);
+}
+
+extern "C" int bgpu_irlba_f32(const float* data_matvec, const void* indices_matvec,
+                              const void* indptr_matvec, const float* data_rmatvec,
+                              const void* indices_rmatvec, const void* indptr_rmatvec,
+                              int index_type, uint64_t num_cells, uint32_t num_genes,
+                              uint32_t k, uint32_t subspace_size, float tolerance,
+                              uint32_t max_iterations, uint64_t seed,
+                              int match_parallel, int is_csr, uint32_t num_threads,
+                              uint64_t chunk_size, float* PCs, int* converged) {
+  (void)data_rmatvec;
+  (void)indices_rmatvec;
+  (void)indptr_rmatvec;
+  BGPU_REQUIRE(!match_parallel || num_threads == 1, BGPU_ERR_INVALID,
+               "match_parallel must be False unless num_threads is 1");
+  BGPU_REQUIRE(num_threads >= 1, BGPU_ERR_INVALID, "num_threads must be >= 1");
+  BGPU_REQUIRE(chunk_size >= 1, BGPU_ERR_INVALID, "chunk_size must be >= 1");
+  BGPU_REQUIRE(index_type == BGPU_INDEX_I32 || index_type == BGPU_INDEX_I64,
+               BGPU_ERR_INVALID, "index_type must be BGPU_INDEX_I32 or _I64");
+  cudaStream_t s = nullptr;
+  const bool have_csr = is_csr || num_threads != 1 || match_parallel;
+  const size_t isz = index_type == BGPU_INDEX_I64 ? 8 : 4;
+  bgpu_matrix_desc d{};
+  d.index_type = index_type;
+  d.value_type = BGPU_VALUE_F32;
+  d.num_cells = num_cells;
+  d.num_genes = num_genes;
+  d.norm_method = BGPU_NORM_NONE;
+  Buf tp, ti, tx, cp, ci, cx;
+  if (have_csr) {
+    int64_t nnz = index_type == BGPU_INDEX_I64
+                      ? ((const int64_t*)indptr_matvec)[num_cells]
+                      : ((const int32_t*)indptr_matvec)[num_cells];
+    d.indptr = indptr_matvec;
+    d.indices = indices_matvec;
+    d.values = data_matvec;
+    d.on_device = 0;
+    d.nnz = (uint64_t)nnz;
+  } else {
+    // The matvec arrays hold the CSC copy (num_genes columns): transpose it on
+    // the GPU (a CSC of X is the CSR of X^T).
+    int64_t nnz = index_type == BGPU_INDEX_I64
+                      ? ((const int64_t*)indptr_matvec)[num_genes]
+                      : ((const int32_t*)indptr_matvec)[num_genes];
+    BGPU_TRY(balloc(cp, (num_genes + 1) * isz, false, s));
+    BGPU_TRY(balloc(ci, nnz * isz, false, s));
+    BGPU_TRY(balloc(cx, nnz * 4, false, s));
+    BGPU_CUDA(cudaMemcpy(cp.p, indptr_matvec, (num_genes + 1) * isz, cudaMemcpyHostToDevice));
+    BGPU_CUDA(cudaMemcpy(ci.p, indices_matvec, nnz * isz, cudaMemcpyHostToDevice));
+    BGPU_CUDA(cudaMemcpy(cx.p, data_matvec, nnz * 4, cudaMemcpyHostToDevice));
+    BGPU_TRY(balloc(tp, (num_cells + 1) * isz, false, s));
+    BGPU_TRY(balloc(ti, nnz * isz, false, s));
+    BGPU_TRY(balloc(tx, nnz * 4, false, s));
+    BGPU_TRY(bgpu_csr_tocsc(num_genes, (uint32_t)std::min<uint64_t>(num_cells, 0xffffffffu),
+                            cp.p, ci.p, cx.p, index_type, tp.p, ti.p, tx.p, s));
+    d.indptr = tp.p;
+    d.indices = ti.p;
+    d.values = tx.p;
+    d.on_device = 1;
+    d.nnz = (uint64_t)nnz;
+  }
+  bgpu_matrix* mat = nullptr;
+  BGPU_TRY(bgpu_matrix_create(&mat, &d, s));
+  bgpu_solve_opts o;
+  bgpu_solve_opts_default(&o);
+  o.k = k;
+  o.subspace_size = subspace_size;
+  o.tolerance = tolerance;
+  o.max_iterations = max_iterations;
+  o.seed = seed;
+  o.chunk_size = chunk_size;
+  bgpu_solve_info info{};
+  int rc = bgpu_irlba(mat, &o, PCs, 0, nullptr, nullptr, &info, s);
+  bgpu_matrix_destroy(mat);
+  if (rc == BGPU_OK && converged) *converged = info.converged;
+  return rc;
+}

@@ -1,0 +1,120 @@
+// Device layout of one cells x genes matrix (internal).
+//
+// HBM layout (n cells, g genes, nnz stored entries):
+//   rowptr      int64[n + 1]              CSR row offsets (shared by both copies:
+//                                          the elements of row panel p occupy
+//                                          [rowptr[p*P], rowptr[(p+1)*P]) in the
+//                                          CSR copy AND in the transposed copy)
+//   kCounts mode (fused normalisation, 4 bytes per stored entry):
+//     csr_packed  uint32[nnz4]            (gene << 16) | count
+//     csc_packed  uint32[nnz4]            (local_row << 16) | count, grouped by
+//                                          row panel, then gene, rows ascending
+//     isf, post   float32[n]              per-cell factors (post may be null)
+//   kFloat mode (pre-normalised values, 6 bytes per stored entry):
+//     csr_val float32[nnz4], csr_col uint16[nnz4]
+//     csc_val float32[nnz4], csc_row uint16[nnz4] (local row within the panel)
+//   colptr      int32[num_panels * (g + 1)] per-panel gene offsets relative to
+//                                          the panel's first element
+// nnz4 = nnz rounded up to a multiple of 4 (+4): every 128-bit load of four
+// entries starting at a multiple of 4 stays inside the allocation.
+#pragma once
+
+#include "common.cuh"
+
+namespace bgpu {
+
+enum MatrixMode { kCounts = 0, kFloat = 1 };
+
+struct Matrix {
+  uint64_t n = 0;
+  uint32_t g = 0;
+  uint64_t nnz = 0;
+  uint64_t nnz_alloc = 0;
+  int mode = kCounts;
+  int norm_method = BGPU_NORM_NONE;
+
+  int64_t* rowptr = nullptr;
+  uint32_t* csr_packed = nullptr;
+  float* csr_val = nullptr;
+  uint16_t* csr_col = nullptr;
+
+  uint32_t pshift = 13;  // log2 of panel rows
+  uint32_t P = 8192;
+  uint32_t num_panels = 0;
+  int32_t* colptr = nullptr;
+  uint32_t* csc_packed = nullptr;
+  float* csc_val = nullptr;
+  uint16_t* csc_row = nullptr;
+
+  float* isf = nullptr;
+  float* post = nullptr;
+
+  float* sd = nullptr;  // cached clipped gene std (computed on first use)
+  int device = 0;
+  uint64_t bytes = 0;
+
+  // Autotuned SpMV shapes (chosen at creation from the nnz-per-row histogram).
+  int spmv_group = 16;     // lanes per row
+  int spmv_blocks = 0;     // CTAs
+  int rmat_colgroup = 256; // genes per CTA in the transposed product
+};
+
+// Per-launch views passed by value to kernels.
+struct CsrView {
+  const int64_t* rowptr;
+  const uint32_t* packed;
+  const float* val;
+  const uint16_t* col;
+  const float* isf;
+  const float* post;
+  uint64_t n;
+  uint32_t g;
+};
+struct CscView {
+  const int64_t* rowptr;
+  const int32_t* colptr;
+  const uint32_t* packed;
+  const float* val;
+  const uint16_t* row;
+  const float* isf;
+  const float* post;
+  uint64_t n;
+  uint32_t g;
+  uint32_t pshift;
+  uint32_t num_panels;
+};
+
+inline CsrView csr_view(const Matrix& m) {
+  return CsrView{m.rowptr, m.csr_packed, m.csr_val, m.csr_col,
+                 m.isf,    m.post,       m.n,       m.g};
+}
+inline CscView csc_view(const Matrix& m) {
+  return CscView{m.rowptr, m.colptr, m.csc_packed, m.csc_val, m.csc_row,
+                 m.isf,    m.post,   m.n,          m.g,       m.pshift,
+                 m.num_panels};
+}
+
+// layout.cu
+int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s);
+void matrix_free(Matrix* m);
+
+// spmv.cu: raw products on the layout (device pointers)
+int launch_matvec(const Matrix& m, const float* v, const float* sd, float* y,
+                  cudaStream_t s);
+// X^T u: per-panel partials (num_panels x g) then a fixed-order reduction.
+// `u_scale_dev` (device scalar, may be null) multiplies u on load; when
+// `u_out` is non-null the normalised u is also written there.
+int launch_rmatvec_partials(const Matrix& m, const float* u,
+                            const float* u_scale_dev, float* u_out,
+                            float* partials, cudaStream_t s);
+int launch_reduce_panels(const Matrix& m, const float* partials,
+                         const float* sd, float* z, cudaStream_t s);
+int launch_gene_stddev(const Matrix& m, double* partials, float* sd,
+                       cudaStream_t s);
+
+// Bytes of the algorithmic traffic of one X.v / X^T.u launch (used for the
+// roofline figure). Counts what the chosen layout must stream.
+double matvec_bytes(const Matrix& m);
+double rmatvec_bytes(const Matrix& m);
+
+}  // namespace bgpu

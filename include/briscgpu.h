@@ -1,0 +1,229 @@
+/*
+ * briscgpu.h -- C ABI of brisc_gb300, a GB300-native (sm_103a) implementation
+ * of brisc's sparse-PCA hot path: SingleCell.pca() -> irlba().
+ *
+ * Plain C: pointers, sizes and an opaque CUDA stream (`void*`, a cudaStream_t;
+ * NULL = the legacy default stream). No torch or numpy types cross this
+ * boundary. Every function returns an int status (BGPU_OK == 0); on failure
+ * bgpu_last_error() returns a message for the calling thread.
+ *
+ * Reference interfaces replaced (paths inside the brisc project):
+ *   brisc/pca.pyx:661-678          irlba(...)                -> bgpu_irlba_f32, bgpu_irlba
+ *   brisc/pca.pyx:440-475          matvec_csr_parallel_raw   -> bgpu_matrix_matvec
+ *   brisc/pca.pyx:478-511          rmatvec_csc_parallel_raw  -> bgpu_matrix_rmatvec
+ *   brisc/pca.pyx:51-103           clipped_stddev_csc        -> bgpu_matrix_gene_stddev
+ *   brisc/pca.pyx:514-545          svd (LAPACK sgesdd)       -> bgpu_small_svd
+ *   brisc/cyutils.pyx:1153-1232,
+ *   brisc/pca.pyx:801-806          PCG32 + Box-Muller start  -> bgpu_start_vector
+ *   brisc/normalize.pyx:9-268      normalize_csr             -> bgpu_normalize_csr,
+ *                                                               bgpu_size_factors
+ *   brisc/cysparse.pyx:1179-1295   csr_tocsc                 -> bgpu_csr_tocsc
+ */
+#ifndef BRISCGPU_H
+#define BRISCGPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define BGPU_API __attribute__((visibility("default")))
+#else
+#define BGPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  BGPU_OK = 0,
+  BGPU_ERR_INVALID = 1,      /* bad argument (mirrors the reference's ValueError) */
+  BGPU_ERR_CUDA = 2,         /* a CUDA runtime call failed                        */
+  BGPU_ERR_ALLOC = 3,        /* device allocation failed                          */
+  BGPU_ERR_UNSUPPORTED = 4,  /* input outside the supported layout limits         */
+  BGPU_ERR_CANCELLED = 5,    /* the cancel flag was raised between restarts       */
+  BGPU_ERR_DEVICE = 6        /* a kernel reported an error status word            */
+};
+
+/* ---- element types of caller arrays ------------------------------------ */
+enum {
+  BGPU_INDEX_I32 = 0,  /* int32 indptr / indices (signed_integer = int)        */
+  BGPU_INDEX_I64 = 1   /* int64 indptr / indices (signed_integer = long long)  */
+};
+enum {
+  BGPU_VALUE_U16 = 0,  /* raw counts, uint16                                   */
+  BGPU_VALUE_U32 = 1,  /* raw counts, uint32 (must be <= 65535)                */
+  BGPU_VALUE_I32 = 2,  /* raw counts, int32  (must be in [0, 65535])           */
+  BGPU_VALUE_F32 = 3   /* float32: already-normalised values, or float counts  */
+};
+
+/* Normalisation applied to the stored values (brisc/normalize.pyx method_number).
+ * BGPU_NORM_NONE: values are already normalised float32 (what pca() receives
+ * after SingleCell.normalize()). The other three fuse the normalisation into
+ * every product: value = log1pf(count * isf[cell]) (* post[cell] for method 2). */
+enum {
+  BGPU_NORM_NONE = -1,
+  BGPU_NORM_LOGCP10K = 0,
+  BGPU_NORM_LOG1PPF = 1,
+  BGPU_NORM_PFLOG1PPF = 2
+};
+
+BGPU_API const char* bgpu_last_error(void);
+BGPU_API const char* bgpu_version(void);
+
+/* ---- device-resident matrix -------------------------------------------- */
+/* A cells x genes CSR matrix laid out for the solver: a packed CSR copy for
+ * X.v and a row-panel transposed (CSC) copy for X^T.u, both built on the GPU,
+ * plus per-cell size factors for the fused normalisation. */
+typedef struct bgpu_matrix bgpu_matrix;
+
+typedef struct bgpu_matrix_desc {
+  const void* indptr;        /* num_cells + 1 entries, index_type              */
+  const void* indices;       /* nnz gene indices, index_type                   */
+  const void* values;        /* nnz values, value_type                         */
+  int index_type;            /* BGPU_INDEX_*                                   */
+  int value_type;            /* BGPU_VALUE_*                                   */
+  int on_device;             /* 1: pointers are device memory; 0: host memory  */
+  uint64_t num_cells;
+  uint32_t num_genes;
+  uint64_t nnz;
+  int norm_method;           /* BGPU_NORM_*                                    */
+  /* Per-cell inverse size factors (float32, num_cells, same memory space as the
+   * arrays above). Required for methods 0-2: the reference computes them from
+   * row sums over ALL genes before HVG subsetting (brisc/normalize.pyx:36-81),
+   * so the caller supplies them (bgpu_size_factors computes them on the GPU). */
+  const float* inv_size_factors;
+  /* Per-cell post-log factors for BGPU_NORM_PFLOG1PPF (normalize.pyx:231-268);
+   * NULL otherwise. */
+  const float* post_factors;
+  /* Rows per transposed panel (power of two in [1024, 65536]); 0 = automatic. */
+  uint32_t panel_rows;
+} bgpu_matrix_desc;
+
+BGPU_API int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* desc,
+                       void* stream);
+BGPU_API int bgpu_matrix_destroy(bgpu_matrix* mat);
+/* Device bytes held by the matrix layout. */
+BGPU_API int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes);
+
+/* y = X . (v / sd)   (brisc/pca.pyx:440-475; no centring). Device pointers.
+ * sd may be NULL (treated as all ones). y has num_cells entries. */
+BGPU_API int bgpu_matrix_matvec(const bgpu_matrix* mat, const float* v, const float* sd,
+                       float* y, void* stream);
+/* z = (X^T . u) / sd  (brisc/pca.pyx:478-511; u assumed zero-mean by the
+ * caller, as there). Device pointers; sd may be NULL. */
+BGPU_API int bgpu_matrix_rmatvec(const bgpu_matrix* mat, const float* u, const float* sd,
+                        float* z, void* stream);
+/* Clipped per-gene sample standard deviation of the normalised values
+ * (brisc/pca.pyx:51-103, clip 1e-8 as pca.pyx:687). Accumulated in FP64. */
+BGPU_API int bgpu_matrix_gene_stddev(const bgpu_matrix* mat, float* sd, void* stream);
+
+/* ---- IRLBA solve ------------------------------------------------------- */
+typedef struct bgpu_solve_opts {
+  uint32_t k;                /* num_PCs                                         */
+  uint32_t subspace_size;    /* m (>= k, <= min(num_cells, num_genes))          */
+  float tolerance;           /* relative residual tolerance                      */
+  uint32_t max_iterations;   /* restarts                                         */
+  uint64_t seed;             /* PCG32 seed of the start vector                   */
+  uint64_t chunk_size;       /* accepted for signature parity: the GPU reduces
+                                over fixed 1024-row blocks whatever its value   */
+  uint32_t reorth_passes;    /* 1 = classical Gram-Schmidt as the reference,
+                                2 = CGS2 (default when 0)                        */
+  uint32_t rotation_mode;    /* 0 = default, 1 = FP32 SIMT GEMM,
+                                2 = tcgen05 3xBF16 split GEMM                    */
+  volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
+                                NULL (replaces PyErr_CheckSignals, pca.pyx:1173) */
+  int use_graphs;            /* replay each Lanczos step from a CUDA graph       */
+  int profile;               /* time the sparse products and the small SVD with
+                                CUDA events (fills the *_seconds fields)         */
+} bgpu_solve_opts;
+
+typedef struct bgpu_solve_info {
+  int32_t converged;
+  uint32_t restarts;         /* IRLBA iterations run                             */
+  uint32_t lanczos_steps;    /* X.v products                                      */
+  uint32_t rmatvecs;         /* X^T.u products                                    */
+  uint32_t num_converged;    /* at the last restart                               */
+  uint32_t k_current;        /* at the last restart                               */
+  double seconds;            /* wall time of the solve (device work included)    */
+  /* Filled when opts.profile is set (CUDA events around each launch group): */
+  double matvec_seconds;     /* summed X.v kernel time                            */
+  double rmatvec_seconds;    /* summed X^T.u kernel time (panel partials)         */
+  double svd_seconds;        /* summed small-SVD time                             */
+  double reorth_seconds;     /* summed U-pass time (dots, updates, norms)         */
+  double vstep_seconds;      /* summed V-side step time                           */
+  double rotation_seconds;   /* summed restart-rotation GEMM time                 */
+  /* Algorithmic bytes of one X.v / X^T.u launch on this layout: */
+  double matvec_bytes;
+  double rmatvec_bytes;
+  double reorth_bytes;       /* summed algorithmic bytes of the U/V passes        */
+  double rotation_bytes;     /* summed algorithmic bytes of the restart rotations */
+  uint64_t kernel_launches;  /* kernels launched by this solve                    */
+} bgpu_solve_info;
+
+BGPU_API void bgpu_solve_opts_default(bgpu_solve_opts* opts);
+
+/* Solve on a device-resident matrix. `pcs` is num_cells x k, C order, float32
+ * (brisc/pca.pyx:678 `PCs`); pcs_on_device selects its memory space.
+ * singular_values (k floats, host) and loadings (num_genes x k, C order,
+ * host; the right singular vectors, V . Vbt^T[:, :k]) may be NULL. */
+BGPU_API int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
+               float* pcs, int pcs_on_device, float* singular_values,
+               float* loadings, bgpu_solve_info* info, void* stream);
+
+/* Drop-in for brisc/pca.pyx:661-678 with the same arguments and meaning: host
+ * arrays, float32 normalised values, CSR for the matvec and (optionally) CSC
+ * for the rmatvec. The CSC arrays may be NULL: the transpose is built on the
+ * GPU either way. `match_parallel` and `num_threads` are validated as the
+ * reference's caller does (single_cell.py:11833-11840) and otherwise unused;
+ * `is_csr` = 0 means the matvec arrays hold a CSC copy (the reference's
+ * num_threads=1 CSC path), which is transposed on the GPU. Writes *converged. */
+BGPU_API int bgpu_irlba_f32(const float* data_matvec, const void* indices_matvec,
+                   const void* indptr_matvec, const float* data_rmatvec,
+                   const void* indices_rmatvec, const void* indptr_rmatvec,
+                   int index_type, uint64_t num_cells, uint32_t num_genes,
+                   uint32_t k, uint32_t subspace_size, float tolerance,
+                   uint32_t max_iterations, uint64_t seed, int match_parallel,
+                   int is_csr, uint32_t num_threads, uint64_t chunk_size,
+                   float* PCs, int* converged);
+
+/* ---- path building blocks (parity-testable individually) ---------------- */
+
+/* V[:, 0] of brisc/pca.pyx:801-806: `num_genes` Box-Muller normals from the
+ * reference's PCG32 (cyutils.pyx:1153-1232), normalised. Host function. */
+BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_host);
+
+/* SVD of one m x (m+1) column-major float32 matrix B (the reference's
+ * `svd(B, Ub, Sb, Vbt, ...)`, pca.pyx:531-545, JOBZ='S'). Device pointers:
+ * Ub m x m, Sb m (descending), Vbt m x (m+1), all column-major. */
+BGPU_API int bgpu_small_svd(const float* B, uint32_t m, float* Ub, float* Sb,
+                   float* Vbt, void* stream);
+
+/* Per-cell normalisation factors (brisc/normalize.pyx:9-268), on the GPU,
+ * over a full-gene counts CSR (device pointers). Writes inverse size factors
+ * `isf` (num_cells floats) and, for method 2, `post` (num_cells floats).
+ * qc_mask (num_cells bytes, nonzero = passed) may be NULL. row_sums (uint64,
+ * num_cells) may be NULL. */
+BGPU_API int bgpu_size_factors(const void* indptr, int index_type, const void* values,
+                      int value_type, uint64_t num_cells, int method,
+                      const uint8_t* qc_mask, float* isf, float* post,
+                      uint64_t* row_sums, void* stream);
+
+/* Materialised normalisation (brisc/normalize.pyx:9 normalize_csr): writes
+ * normalized[nnz] = log1pf(count * isf[row]) (* post[row]). Device pointers. */
+BGPU_API int bgpu_normalize_csr(const void* indptr, int index_type, const void* values,
+                       int value_type, uint64_t num_cells, const float* isf,
+                       const float* post, float* normalized, void* stream);
+
+/* Stable CSR -> CSC transpose (brisc/cysparse.pyx:1179-1295): rows ascending
+ * within each column. Device pointers; Ap/Aj/Bp/Bi share index_type; Ax/Bx
+ * are 4-byte values (float32/int32/uint32) copied bit for bit. */
+BGPU_API int bgpu_csr_tocsc(uint64_t n_row, uint32_t n_col, const void* Ap,
+                   const void* Aj, const void* Ax, int index_type, void* Bp,
+                   void* Bi, void* Bx, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRISCGPU_H */

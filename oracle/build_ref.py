@@ -1,0 +1,136 @@
+"""Build the reference's own CPU implementation of the sparse-PCA path.
+
+Test and baseline infrastructure only: the product never imports it.
+
+Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
+
+1. ``cythonize`` (needs Cython and the reference checkout): translate the
+   reference modules on the path -- ``brisc/cyutils.pyx``, ``brisc/pca.pyx``,
+   ``brisc/normalize.pyx``, ``brisc/cysparse.pyx`` -- plus the test harness
+   ``oracle/ref_probe.pyx`` to C++ under ``oracle/_ref/gen/``. The sources are
+   read where they lie; nothing is copied into the repository.
+2. ``compile`` (needs only g++, Python and numpy headers): build every
+   ``oracle/_ref/gen/*.cpp`` into ``oracle/_ref/<machine>/brisc/*.so`` with the
+   reference's own Linux flags (``setup.py:92-100`` of the reference:
+   ``-Ofast -funroll-loops -std=c++17 -fopenmp`` plus the baseline ``-march``
+   variant of the machine, ``setup.py:38-45``).
+
+Stage 2 runs on any machine that received ``oracle/_ref/gen`` (the C++ is
+architecture-neutral), so the aarch64 GPU host can rebuild the reference
+without Cython.
+
+Usage::
+
+    python oracle/build_ref.py [--reference DIR] [--jobs N] [--compile-only]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import platform
+import subprocess
+import sys
+import sysconfig
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_OUT = HERE / "_ref"
+GEN = REF_OUT / "gen"
+MODULES = ["cyutils", "pca", "normalize", "cysparse"]
+# What the CPU baseline needs (cysparse's 24 MB of C++ is only needed for the
+# transpose fixture and is skipped where compile time matters).
+BASELINE_MODULES = ["cyutils", "pca", "normalize", "ref_probe"]
+DIRECTIVES = {"language_level": "3", "boundscheck": False,
+              "wraparound": False, "cdivision": True,
+              "initializedcheck": False, "warn.undeclared": False}
+
+
+def machine_dir() -> Path:
+    return REF_OUT / platform.machine().lower()
+
+
+def march_flag() -> list[str]:
+    m = platform.machine().lower()
+    if m in ("x86_64", "amd64"):
+        return ["-march=x86-64-v3"]
+    if m == "aarch64":
+        return ["-march=armv8.2-a"]
+    return []
+
+
+def cythonize(reference: Path) -> None:
+    from Cython.Compiler.Main import CompilationOptions, compile_single
+    GEN.mkdir(parents=True, exist_ok=True)
+    jobs = [(reference / "brisc" / f"{m}.pyx", GEN / f"brisc.{m}.cpp")
+            for m in MODULES]
+    jobs.append((HERE / "ref_probe.pyx", GEN / "brisc.ref_probe.cpp"))
+    for src, out in jobs:
+        if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+            continue
+        opts = CompilationOptions(
+            cplus=True, output_file=str(out), language_level=3,
+            include_path=[str(reference)], compiler_directives=DIRECTIVES)
+        if src.parent == HERE:
+            # The harness is compiled as the module `brisc.ref_probe`.
+            opts.module_name = "brisc.ref_probe"
+        res = compile_single(str(src), opts,
+                             full_module_name="brisc." + src.stem)
+        if res.num_errors:
+            raise RuntimeError(f"cython failed on {src}")
+        print(f"cythonized {src.name} -> {out.relative_to(HERE)}")
+
+
+def compile_all(jobs: int, modules: list[str] | None = None) -> Path:
+    import numpy as np
+    out_pkg = machine_dir() / "brisc"
+    out_pkg.mkdir(parents=True, exist_ok=True)
+    (out_pkg / "__init__.py").write_text("")
+    ext = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    inc = [sysconfig.get_paths()["include"], np.get_include()]
+    flags = ["-Ofast", "-funroll-loops", "-std=c++17", "-g0", "-fopenmp",
+             "-fPIC", "-shared", "-w",
+             "-DNPY_NO_DEPRECATED_API=NPY_1_17_API_VERSION",
+             *march_flag(), *[f"-I{i}" for i in inc]]
+    cpps = sorted(GEN.glob("brisc.*.cpp"))
+    if modules is not None:
+        cpps = [c for c in cpps if c.stem.split(".", 1)[1] in modules]
+    if not cpps:
+        raise FileNotFoundError(
+            f"no generated C++ under {GEN}; run the cythonize stage where "
+            "the reference checkout and Cython are available")
+
+    def one(cpp: Path) -> str:
+        mod = cpp.stem.split(".", 1)[1]
+        so = out_pkg / f"{mod}{ext}"
+        if so.exists() and so.stat().st_mtime >= cpp.stat().st_mtime:
+            return f"up to date {so.name}"
+        cmd = ["g++", *flags, str(cpp), "-o", str(so), "-fopenmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"g++ failed on {cpp.name}:\n{r.stderr[-4000:]}")
+        return f"built {so.relative_to(HERE)}"
+
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        for msg in ex.map(one, cpps):
+            print(msg)
+    return machine_dir()
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    ap.add_argument("--compile-only", action="store_true")
+    ap.add_argument("--baseline-only", action="store_true",
+                    help="compile only the modules the CPU baseline needs")
+    a = ap.parse_args(argv)
+    ref = Path(a.reference)
+    if not a.compile_only and (ref / "brisc" / "pca.pyx").exists():
+        cythonize(ref)
+    compile_all(a.jobs, BASELINE_MODULES if a.baseline_only else None)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,137 @@
+"""ORACLE (test/baseline infrastructure): the reference's own compiled modules.
+
+``load()`` imports brisc's ``pca``, ``normalize``, ``cysparse`` and the
+``ref_probe`` harness from ``oracle/_ref/<machine>/`` (built by
+oracle/build_ref.py from the reference checkout, or from the generated C++
+that travels with the repository when no checkout is present). Returns None
+when neither is available.
+
+``run_irlba`` calls the reference's ``irlba`` exactly as ``SingleCell.pca()``
+does (brisc/single_cell.py:12037-12091): CSR for the matvec, the reference's
+own ``csr_tocsc`` for the rmatvec copy, ``match_parallel=False``, inside
+``threadpool_limits(1, 'blas')`` when threadpoolctl is available.
+"""
+from __future__ import annotations
+
+import contextlib
+import importlib
+import os
+import platform
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_mods = None
+
+
+def _machine_dir() -> Path:
+    return HERE / "_ref" / platform.machine().lower()
+
+
+def available() -> bool:
+    return (_machine_dir() / "brisc").exists() or (HERE / "_ref" / "gen").exists()
+
+
+def load(build: bool = True):
+    global _mods
+    if _mods is not None:
+        return _mods
+    d = _machine_dir()
+    pkg = d / "brisc"
+    have = pkg.exists() and any(pkg.glob("pca*.so"))
+    if not have and build:
+        from . import build_ref
+        ref = Path("/root/reference")
+        try:
+            if (ref / "brisc" / "pca.pyx").exists():
+                build_ref.cythonize(ref)
+            build_ref.compile_all(os.cpu_count() or 4,
+                                  modules=build_ref.BASELINE_MODULES)
+        except Exception as e:  # noqa: BLE001 - reported to the caller
+            print(f"[oracle.ref] reference build unavailable: {e}", file=sys.stderr)
+            return None
+        have = any(pkg.glob("pca*.so"))
+    if not have:
+        return None
+    if str(d) not in sys.path:
+        sys.path.insert(0, str(d))
+    _mods = {}
+    for name in ("cyutils", "pca", "normalize", "cysparse", "ref_probe"):
+        try:
+            _mods[name] = importlib.import_module(f"brisc.{name}")
+        except ImportError:
+            if name != "cysparse":
+                raise
+    return _mods
+
+
+@contextlib.contextmanager
+def _blas1():
+    try:
+        from threadpoolctl import threadpool_limits
+    except ImportError:
+        yield
+        return
+    with threadpool_limits(1, user_api="blas"):
+        yield
+
+
+def tocsc(indptr, indices, data, n_row: int, n_col: int, num_threads: int):
+    """The reference's csr_tocsc (brisc/cysparse.pyx:1179) on int32/int64 arrays."""
+    M = load()
+    Bp = np.empty(n_col + 1, dtype=indptr.dtype)
+    Bi = np.empty(indices.shape[0], dtype=indices.dtype)
+    Bx = np.empty(data.shape[0], dtype=data.dtype)
+    # bit views, as brisc/sparse.py:933-934 passes them (fused type bit_width)
+    bits = np.uint32 if data.dtype.itemsize == 4 else np.uint64
+    M["cysparse"].csr_tocsc(n_row, n_col, indptr, indices, data.view(bits), Bp,
+                            Bi, Bx.view(bits), num_threads)
+    return Bp, Bi, Bx
+
+
+def normalize(indptr, indices, data, method: int, num_threads: int, qc=None):
+    """The reference's normalize_csr (brisc/normalize.pyx:9)."""
+    M = load()
+    n = indptr.shape[0] - 1
+    out = np.empty(data.shape[0], dtype=np.float32)
+    rs = np.empty(n, dtype=np.uint64)
+    q = np.array([], dtype=bool) if qc is None else np.ascontiguousarray(qc, dtype=bool)
+    M["normalize"].normalize_csr(data, indices, indptr, q.view(np.int8), out, rs,
+                                 n, method, num_threads)
+    return out, rs
+
+
+def run_irlba(indptr, indices, data_f32, n: int, g: int, k: int = 50,
+              m: int = 100, tol: float = 1e-6, max_iterations: int = 100,
+              seed: int = 0, num_threads: int | None = None,
+              chunk_size: int = 1024, csc=None, match_parallel=None):
+    """Returns (PCs, converged). `csc` = (indptr, indices, data) to reuse.
+
+    Array selection follows brisc/single_cell.py:12037-12055 for CSR input:
+    the rmatvec gets the CSC copy unless num_threads == 1 and not
+    match_parallel, where it gets the CSR arrays again. match_parallel
+    defaults to True for one thread (the reference tests' golden setting,
+    tests/test_pca.py:9-10), so every thread count runs the same arithmetic.
+    """
+    M = load()
+    num_threads = num_threads or os.cpu_count() or 1
+    if match_parallel is None:
+        match_parallel = num_threads == 1
+    m = min(m, n, g)
+    serial = num_threads == 1 and not match_parallel
+    if serial:
+        csc = (indptr, indices, data_f32)
+    elif csc is None:
+        csc = tocsc(indptr, indices, data_f32, n, g, num_threads)
+    PCs = np.zeros((n, k), dtype=np.float32)
+    with _blas1():
+        conv = M["pca"].irlba(
+            data_matvec=data_f32, indices_matvec=indices, indptr_matvec=indptr,
+            data_rmatvec=csc[2], indices_rmatvec=csc[1], indptr_rmatvec=csc[0],
+            num_cells=n, num_genes=g, k=k, subspace_size=m, tolerance=tol,
+            max_iterations=max_iterations, seed=seed,
+            match_parallel=bool(match_parallel), is_csr=True,
+            num_threads=num_threads, chunk_size=chunk_size, PCs=PCs)
+    return PCs, bool(conv)

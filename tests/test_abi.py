@@ -1,0 +1,83 @@
+"""The C-ABI library loads and exports every symbol include/briscgpu.h declares.
+
+CPU only: no call here launches a kernel. Host-only entry points (the start
+vector) and argument validation are exercised directly.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "briscgpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bgpu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_path():
+    names = declared_functions()
+    for must in ["bgpu_irlba", "bgpu_irlba_f32", "bgpu_matrix_create",
+                 "bgpu_matrix_matvec", "bgpu_matrix_rmatvec", "bgpu_small_svd",
+                 "bgpu_csr_tocsc", "bgpu_normalize_csr", "bgpu_size_factors",
+                 "bgpu_start_vector", "bgpu_matrix_gene_stddev"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(str(built_lib))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(built_lib):
+    from brisc_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_version_and_error_string(built_lib):
+    from brisc_gb300 import _lib
+    L = _lib.lib()
+    assert b"sm_103a" in L.bgpu_version()
+    assert isinstance(L.bgpu_last_error(), bytes)
+
+
+def test_host_start_vector_matches_reference(built_lib, golden):
+    """bgpu_start_vector is host code: bit-exact normals, norm within ulps."""
+    from brisc_gb300 import _lib
+    z = golden("rng")
+    out = np.empty(2000, dtype=np.float32)
+    i = 0
+    while f"seed_{i}" in z.files:
+        _lib.call("bgpu_start_vector", int(z[f"seed_{i}"]), 2000, out.ctypes.data)
+        d = np.abs(out.view(np.int32).astype(np.int64) -
+                   z[f"start_{i}"].view(np.int32).astype(np.int64))
+        assert d.max() <= 8
+        i += 1
+
+
+def test_invalid_arguments_rejected_without_gpu(built_lib):
+    from brisc_gb300 import _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    assert L.bgpu_matrix_create(C.byref(h), None, None) == _lib.ERR_INVALID
+    assert b"desc" in L.bgpu_last_error()
+    o = _lib.SolveOpts()
+    L.bgpu_solve_opts_default(C.byref(o))
+    assert (o.k, o.subspace_size, o.max_iterations) == (50, 100, 100)
+    assert abs(o.tolerance - 1e-6) < 1e-12 and o.reorth_passes == 2
+    assert L.bgpu_irlba(None, C.byref(o), None, 0, None, None, None, None) == _lib.ERR_INVALID
+    d = _lib.MatrixDesc()
+    d.num_cells, d.num_genes = 10, 70000
+    d.indptr = 1
+    assert L.bgpu_matrix_create(C.byref(h), C.byref(d), None) == _lib.ERR_UNSUPPORTED
+    d.num_genes = 10
+    d.index_type = 7
+    assert L.bgpu_matrix_create(C.byref(h), C.byref(d), None) == _lib.ERR_INVALID
+    with pytest.raises(ValueError):
+        _lib.call("bgpu_start_vector", 0, 0, None)

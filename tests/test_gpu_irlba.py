@@ -1,0 +1,170 @@
+"""End-to-end IRLBA on the GPU vs the reference's own outputs and FP64.
+
+Tolerances (the accuracy gates of this path): relative singular-value error
+<= 1e-4, max principal angle <= 1e-3 rad on subspaces with a spectral gap,
+sign-aligned per-PC cosine >= 1 - 1e-4 against the reference's PCs on the
+gapped fixtures, and run-to-run bit identity.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import brisc_gb300 as bg
+from brisc_gb300 import DeviceMatrix, _lib
+from brisc_gb300.synth import nb_counts
+from oracle import dense
+from oracle import irlba as oirlba
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(z, name):
+    n, g, k, m = (int(v) for v in z[f"{name}_shape"])
+    X = sp.csr_matrix((z[f"{name}_data"], z[f"{name}_indices"],
+                       z[f"{name}_indptr"]), shape=(n, g))
+    return X, n, g, k, m
+
+
+def _cos(a, b):
+    a = dense.align_signs(a, b)
+    return np.sum(a * b, 0) / np.linalg.norm(a, axis=0) / np.linalg.norm(b, axis=0)
+
+
+@pytest.mark.parametrize("name", ["clustered_a", "clustered_b"])
+def test_dropin_irlba_matches_reference(cuda, golden, name):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, name)
+    ref = z[f"{name}_pcs"]
+    PCs = np.empty((n, k), dtype=np.float32)
+    csc = X.tocsc()
+    conv = bg.irlba(data_matvec=X.data, indices_matvec=X.indices,
+                    indptr_matvec=X.indptr, data_rmatvec=csc.data,
+                    indices_rmatvec=csc.indices, indptr_rmatvec=csc.indptr,
+                    num_cells=n, num_genes=g, k=k, subspace_size=m,
+                    tolerance=1e-6, max_iterations=100, seed=0,
+                    match_parallel=False, is_csr=True, num_threads=8,
+                    chunk_size=1024, PCs=PCs)
+    assert conv == bool(z[f"{name}_converged"])
+    s_ref, s = dense.sv_from_pcs(ref), dense.sv_from_pcs(PCs)
+    assert np.max(np.abs(s - s_ref) / s_ref) < 1e-4
+    assert dense.max_angle(PCs, ref) < 1e-3
+    assert _cos(PCs, ref).min() > 1 - 1e-4
+    S, U, Vt = dense.top_svd(X, k + 2)
+    assert dense.rel_sv_error(PCs, S).max() < 1e-4
+    j = max(dense.gap_mask(S, k, 0.01))
+    assert dense.max_angle(PCs[:, :j], U[:, :j]) < 1e-3
+
+
+def test_bit_identical_runs(cuda, golden):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_a")
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    a = M.solve(k, m)
+    b = M.solve(k, m)
+    M.close()
+    M2 = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    c = M2.solve(k, m)
+    M2.close()
+    assert np.array_equal(a.PCs, b.PCs) and np.array_equal(a.PCs, c.PCs)
+    assert np.array_equal(a.singular_values, c.singular_values)
+
+
+@pytest.mark.parametrize("passes", [1, 2])
+def test_reorth_passes_both_meet_gates(cuda, golden, passes):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_b")
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    r = M.solve(k, m, reorth_passes=passes, loadings=True)
+    M.close()
+    S, U, Vt = dense.top_svd(X, k + 2)
+    assert r.converged
+    assert dense.rel_sv_error(r.PCs, S).max() < 1e-4
+    np.testing.assert_allclose(r.singular_values, dense.sv_from_pcs(r.PCs), rtol=1e-4)
+    # loadings are the right singular vectors: A^T u = s v
+    assert dense.max_angle(r.loadings, Vt.T[:, :k]) < 1e-3
+    assert dense.residuals(X, r.PCs).max() < 1e-3
+
+
+def test_flat_spectrum_singular_values(cuda, golden):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "flat")
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    r = M.solve(k, m)
+    M.close()
+    S, U, Vt = dense.top_svd(X, k + 2)
+    assert dense.rel_sv_error(r.PCs, S).max() < 1e-4
+    assert dense.rel_sv_error(z["flat_pcs"], S).max() < 1e-4
+
+
+@pytest.mark.parametrize("method", ["logCP10k", "log1pPF", "PFlog1pPF"])
+def test_fused_counts_path_matches_materialised(cuda, golden, method):
+    """PCA on raw counts with the normalisation fused into every product
+    equals PCA on the normalised float32 matrix (the reference's route)."""
+    from oracle import clib
+    z = golden("irlba")
+    ip, ix, cnt = z["clustered_a_indptr"], z["clustered_a_indices"], z["clustered_a_counts"]
+    n, g, k, m = (int(v) for v in z["clustered_a_shape"])
+    counts = sp.csr_matrix((cnt, ix, ip), shape=(n, g))
+    mnum = {"logCP10k": 0, "log1pPF": 1, "PFlog1pPF": 2}[method]
+    xn, rs, isf, post = clib.normalize_csr(ip, cnt, mnum)
+    Xn = sp.csr_matrix((xn, ix, ip), shape=(n, g))
+    pcs_f, rf = bg.pca(Xn, num_PCs=k, subspace_size=m, return_result=True)
+    pcs_c, rc = bg.pca_counts(counts, method=method, num_PCs=k, subspace_size=m,
+                              return_result=True)
+    s_f, s_c = dense.sv_from_pcs(pcs_f), dense.sv_from_pcs(pcs_c)
+    assert np.max(np.abs(s_c - s_f) / s_f) < 1e-5
+    assert dense.max_angle(pcs_c, pcs_f) < 1e-3
+
+
+def test_pca_qc_backfill_and_joint(cuda, golden):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_a")
+    qc = (np.arange(n) % 9) != 4
+    pcs = bg.pca(X, QC_column=qc, num_PCs=k, subspace_size=m)
+    assert pcs.shape == (n, k) and np.isnan(pcs[~qc]).all()
+    sub = bg.pca(X[np.flatnonzero(qc)], num_PCs=k, subspace_size=m)
+    assert np.array_equal(pcs[qc], sub)
+    a, b = bg.pca(X[: n // 2], X[n // 2:], num_PCs=k, subspace_size=m)
+    joint = bg.pca(X, num_PCs=k, subspace_size=m)
+    assert np.array_equal(np.vstack([a, b]), joint)
+
+
+def test_nonconverged_returns_ritz_vectors(cuda, golden):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_a")
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    r = M.solve(k, m, max_iterations=1)
+    M.close()
+    o = oirlba.irlba(X, k, m, max_iterations=1, reorth_passes=2)
+    assert not r.converged and not o["converged"]
+    s, so = dense.sv_from_pcs(r.PCs), dense.sv_from_pcs(o["PCs"])
+    assert np.max(np.abs(s - so) / so) < 1e-4
+    np.testing.assert_allclose(s, r.singular_values, rtol=1e-5)
+
+
+def test_small_problem_full_subspace(cuda):
+    c = nb_counts(60, 12, seed=8, density=0.3, workers=1)
+    X = sp.csr_matrix((c.normalized_f32(), c.indices, c.indptr), shape=(c.num_cells, 12))
+    pcs = bg.pca(X, num_PCs=5, subspace_size=100)  # clipped to min(n, g) = 12
+    S, U, Vt = dense.top_svd(X, 5)
+    assert dense.rel_sv_error(pcs, S).max() < 1e-4
+
+
+def test_cancel_flag(cuda, golden):
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_a")
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    flag = C.c_int32(1)
+    o = _lib.SolveOpts()
+    _lib.lib().bgpu_solve_opts_default(C.byref(o))
+    o.k, o.subspace_size = k, m
+    o.cancel = C.cast(C.pointer(flag), C.c_void_p)
+    pcs = np.empty((n, k), dtype=np.float32)
+    rc = _lib.lib().bgpu_irlba(M.handle, C.byref(o), pcs.ctypes.data, 0, None,
+                               None, None, None)
+    assert rc == _lib.ERR_CANCELLED
+    r = M.solve(k, m)  # the context stays usable
+    assert r.converged
+    M.close()

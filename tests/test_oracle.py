@@ -1,0 +1,113 @@
+"""The oracle pinned against the reference's own outputs (tests/golden/).
+
+CPU only. Integer and byte work must match bit for bit; float work within the
+stated tolerance.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import clib, dense
+from oracle import irlba as oirlba
+
+
+def _ulp(a, b):
+    return int(np.max(np.abs(a.view(np.int32).astype(np.int64) -
+                             b.view(np.int32).astype(np.int64))))
+
+
+def test_pcg32_and_box_muller_bit_exact(golden):
+    z = golden("rng")
+    i = 0
+    while f"seed_{i}" in z.files:
+        seed = int(z[f"seed_{i}"])
+        assert np.array_equal(clib.raw_rand(seed, 64), z[f"rand_{i}"])
+        assert np.array_equal(clib.raw_normals(seed, 4096), z[f"normals_{i}"])
+        i += 1
+    assert i >= 5
+
+
+def test_start_vector_within_ulps(golden):
+    # The normals are bit-exact; the reference binary sums the squares for the
+    # norm in vectorised order (-Ofast), so the normalised vector may differ
+    # by a few ulp from the sequential sum written in pca.pyx:804.
+    z = golden("rng")
+    i = 0
+    while f"seed_{i}" in z.files:
+        seed = int(z[f"seed_{i}"])
+        sv = clib.start_vector(seed, 2000)
+        assert _ulp(sv, z[f"start_{i}"]) <= 8
+        i += 1
+    assert _ulp(clib.start_vector(0, 37), z["start_small"]) <= 8
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+@pytest.mark.parametrize("tag", ["all", "qc"])
+def test_normalize_bit_exact(golden, method, tag):
+    z = golden("normalize")
+    qc = z["qc"] if tag == "qc" else None
+    out, rs, isf, post = clib.normalize_csr(z["indptr"], z["counts"], method, qc)
+    assert np.array_equal(rs, z[f"rowsums_{tag}"])
+    assert np.array_equal(out, z[f"m{method}_{tag}"])
+
+
+def test_csr_tocsc_bit_exact(golden):
+    z = golden("tocsc")
+    bp, bi, bx = clib.csr_tocsc(z["indptr"], z["indices"], z["data"], int(z["n_col"]))
+    assert np.array_equal(bp, z["Bp"]) and np.array_equal(bi, z["Bi"])
+    assert np.array_equal(bx.view(np.uint32), z["Bx"].view(np.uint32))
+    assert np.array_equal(z["Bp"], z["Bp64"]) and np.array_equal(z["Bi"], z["Bi64"])
+
+
+def test_thread_offsets_balance():
+    ip = np.array([0, 5, 5, 9, 30, 31, 40, 41, 60], dtype=np.int64)
+    off = clib.thread_offsets(ip, 3)
+    assert off[0] == 0 and off[-1] == 8 and np.all(np.diff(off.astype(int)) >= 0)
+
+
+def _case(z, name):
+    n, g, k, m = (int(v) for v in z[f"{name}_shape"])
+    X = sp.csr_matrix((z[f"{name}_data"], z[f"{name}_indices"], z[f"{name}_indptr"]),
+                      shape=(n, g))
+    return X, k, m
+
+
+@pytest.mark.parametrize("name", ["clustered_a", "clustered_b"])
+def test_oracle_irlba_matches_reference(golden, name):
+    z = golden("irlba")
+    X, k, m = _case(z, name)
+    ref_pcs = z[f"{name}_pcs"]
+    o = oirlba.irlba(X, k, m)
+    assert o["converged"] == bool(z[f"{name}_converged"])
+    s_ref = dense.sv_from_pcs(ref_pcs)
+    s_or = dense.sv_from_pcs(o["PCs"])
+    assert np.max(np.abs(s_or - s_ref) / s_ref) < 1e-5
+    assert dense.max_angle(o["PCs"], ref_pcs) < 1e-3
+    # sign-aligned per-PC agreement
+    a = dense.align_signs(o["PCs"], ref_pcs)
+    cos = np.sum(a * ref_pcs, 0) / np.linalg.norm(a, axis=0) / np.linalg.norm(ref_pcs, axis=0)
+    assert np.min(cos) > 1 - 1e-5
+
+
+def test_reference_vs_fp64(golden):
+    """Pins the FP64 oracle: the reference's PCs meet the accuracy gates on
+    the gapped fixtures (rel SV <= 1e-4; principal angle <= 1e-3 rad)."""
+    z = golden("irlba")
+    for name in ["clustered_a", "clustered_b"]:
+        X, k, m = _case(z, name)
+        S, U, Vt = dense.top_svd(X, k + 2)
+        pcs = z[f"{name}_pcs"]
+        assert dense.rel_sv_error(pcs, S).max() < 1e-4
+        gaps = dense.gap_mask(S, k, 0.01)
+        assert gaps, "fixture should have separated singular values"
+        j = max(gaps)
+        assert dense.max_angle(pcs[:, :j], U[:, :j]) < 1e-3
+
+
+def test_flat_spectrum_singular_values(golden):
+    z = golden("irlba")
+    X, k, m = _case(z, "flat")
+    S, U, Vt = dense.top_svd(X, k + 2)
+    o = oirlba.irlba(X, k, m, reorth_passes=2)
+    assert dense.rel_sv_error(z["flat_pcs"], S).max() < 1e-4
+    assert dense.rel_sv_error(o["PCs"], S).max() < 1e-4
