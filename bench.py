@@ -305,8 +305,11 @@ def run_ours(args):
                                    infos[0]["rmatvec_bytes"] * tot("rmatvecs")),
         "u_pass (dots/update)": (tot("reorth_seconds"), tot("reorth_bytes")),
         "restart_rotation": (tot("rotation_seconds"), tot("rotation_bytes")),
+        "v_step": (tot("vstep_seconds"), 0.0),
+        "small_svd": (tot("svd_seconds"), 0.0),
     }
-    dominant = max(classes, key=lambda c: classes[c][0])
+    dominant = max((c for c in classes if classes[c][1] > 0),
+                   key=lambda c: classes[c][0])
     secs, byts = classes[dominant]
     achieved = byts / secs / 1e9 if secs > 0 else None
     sp_secs = tot("matvec_seconds") + tot("rmatvec_seconds")

@@ -12,6 +12,8 @@
 // here the last restart is not rotated, so the returned PCs are the Ritz
 // vectors of the final SVD, scaled by their singular values.
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -136,7 +138,9 @@ struct Solver {
   float tol;
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, rem, sd, Bf, Ub, Sb, Vbt,
-      svdwork, scal, smax, B, st, sdpart, svdinfo;
+      svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last, sb64, ratios;
+  bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
+  bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
   PinnedStatus hst;
 
   // accounting
@@ -211,8 +215,11 @@ struct Solver {
     BGPU_TRY(balloc(Ub, (size_t)m * m * 4, true, s));
     BGPU_TRY(balloc(Sb, (size_t)m * 4, true, s));
     BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
-    if (jacobi_smem_bytes(m) > 220 * 1024)
-      BGPU_TRY(balloc(svdwork, jacobi_global_floats(m) * 4, true, s));
+    if (jacobi_smem_bytes(m, svd64) > 220 * 1024)
+      BGPU_TRY(balloc(svdwork, jacobi_global_bytes(m, svd64), true, s));
+    BGPU_TRY(balloc(ub_last, (size_t)m * 8, true, s));
+    BGPU_TRY(balloc(sb64, (size_t)m * 8, true, s));
+    BGPU_TRY(balloc(ratios, (size_t)m * 4, true, s));
     BGPU_TRY(balloc(scal, 64, true, s));
     BGPU_TRY(balloc(smax, 64, false, s));
     BGPU_TRY(balloc(B, (size_t)m * (m + 1) * 8, true, s));
@@ -312,6 +319,11 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
 
   Solver S(X, o, s);
   S.profile = o.profile != 0;
+  {
+    S.svd64 = o.svd_fp64 != 0;
+    const char* et = std::getenv("BGPU_TRACE");
+    S.trace = et && et[0] == '1';
+  }
   BGPU_TRY(S.alloc());
   const uint32_t m = S.m, k = S.k, g = S.g;
 
@@ -341,22 +353,48 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
       ++steps;
     }
     ++restarts;
-    BGPU_TRY(launch_b_to_float(S.B.as<double>(), m, S.Bf.as<float>(), s));
     BGPU_TRY(S.ev_begin(2));
-    BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), m, S.Ub.as<float>(),
-                               S.Sb.as<float>(), S.Vbt.as<float>(),
-                               S.svdwork.as<float>(), S.svdinfo.as<int>(), s));
+    if (S.svd64) {
+      BGPU_TRY(launch_jacobi_svd(nullptr, S.B.as<double>(), m, S.Ub.as<float>(),
+                                 S.Sb.as<float>(), S.Vbt.as<float>(),
+                                 S.ub_last.as<double>(), S.sb64.as<double>(),
+                                 S.svdwork.p, S.svdinfo.as<int>(), s));
+      S.launches += 2;
+    } else {
+      BGPU_TRY(launch_b_to_float(S.B.as<double>(), m, S.Bf.as<float>(), s));
+      BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), nullptr, m, S.Ub.as<float>(),
+                                 S.Sb.as<float>(), S.Vbt.as<float>(), nullptr,
+                                 nullptr, S.svdwork.p, S.svdinfo.as<int>(), s));
+      S.launches += 3;
+    }
     BGPU_TRY(S.ev_end());
-    S.launches += 3;
-    BGPU_TRY(launch_restart_check(S.Ub.as<float>(), S.Sb.as<float>(), m, k,
-                                  S.rem.as<float>(), g, o.tolerance,
-                                  S.smax.as<float>(), kc, S.B.as<double>(),
-                                  S.st.as<RestartStatus>(), s));
+    BGPU_TRY(launch_restart_check(
+        S.Ub.as<float>(), S.Sb.as<float>(),
+        S.svd64 ? S.ub_last.as<double>() : nullptr,
+        S.svd64 ? S.sb64.as<double>() : nullptr, m, k, S.rem.as<float>(), g,
+        o.tolerance, S.smax.as<float>(), kc, S.B.as<double>(),
+        S.st.as<RestartStatus>(), S.trace ? S.ratios.as<float>() : nullptr, s));
     BGPU_CUDA(cudaMemcpyAsync(S.hst.h, S.st.p, sizeof(RestartStatus),
                               cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaStreamSynchronize(s));
     BGPU_TRY(S.ev_collect());
     last = *S.hst.h;
+    if (S.trace) {
+      std::vector<float> rat(k);
+      int sw[2] = {0, 0};
+      BGPU_CUDA(cudaMemcpy(rat.data(), S.ratios.p, k * 4, cudaMemcpyDeviceToHost));
+      BGPU_CUDA(cudaMemcpy(sw, S.svdinfo.p, 8, cudaMemcpyDeviceToHost));
+      float worst_conv = 0.f, best_open = 1e30f;
+      for (float r : rat) {
+        if (r < 1.f) worst_conv = std::max(worst_conv, r);
+        else best_open = std::min(best_open, r);
+      }
+      std::fprintf(stderr,
+                   "[bgpu] restart %u steps %u kc %u -> %d nconv %d rn %.6g "
+                   "smax %.6g sweeps %d conv-ratio max %.3g open-ratio min %.3g\n",
+                   it, steps, kc, last.k_current, last.num_converged,
+                   last.remainder_norm, last.smax, sw[0], worst_conv, best_open);
+    }
     if (last.converged) { converged = true; break; }
     if (it + 1 == o.max_iterations) break;
     kc = (uint32_t)last.k_current;

@@ -34,24 +34,37 @@ __device__ __forceinline__ void pair_of(int round, int idx, int M2, int* p,
   *q = max(a, b);
 }
 
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// T = float (FP32 Jacobi) or double (FP64 Jacobi). B is read in T; outputs are
+// float (for the rotation GEMMs) plus, when non-null, the FP64 last row of Ub
+// and FP64 singular values for the convergence test.
+template <typename T>
 __global__ void __launch_bounds__(1024)
-k_jacobi(const float* __restrict__ Bf, uint32_t m, float* __restrict__ Ub,
+k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
          float* __restrict__ Sb, float* __restrict__ Vbt,
-         float* __restrict__ gwork, int use_smem, int max_sweeps, float thresh,
+         double* __restrict__ ub_last, double* __restrict__ sb64,
+         T* __restrict__ gwork, int use_smem, int max_sweeps, T thresh,
          int* __restrict__ info) {
-  extern __shared__ float sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int rotated;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int la = (int)m + 1;  // column length of A = B^T
-  float* A = use_smem ? sm : gwork;
-  float* J = A + (uint64_t)m * la;
+  T* A = use_smem ? reinterpret_cast<T*>(smraw) : gwork;
+  T* J = A + (uint64_t)m * la;
+  T* sig = J + (uint64_t)m * m;
   for (uint32_t t = threadIdx.x; t < m * (uint32_t)la; t += blockDim.x) {
     const uint32_t i = t / la, r = t % la;   // A[r, i] = B[i, r]
-    A[(uint64_t)i * la + r] = Bf[i + (uint64_t)r * m];
+    A[(uint64_t)i * la + r] = Bin[i + (uint64_t)r * m];
   }
   for (uint32_t t = threadIdx.x; t < m * m; t += blockDim.x)
-    J[t] = (t / m == t % m) ? 1.f : 0.f;
+    J[t] = (t / m == t % m) ? T(1) : T(0);
   __syncthreads();
 
   const int M2 = (int)m + ((int)m & 1);
@@ -64,35 +77,34 @@ k_jacobi(const float* __restrict__ Bf, uint32_t m, float* __restrict__ Ub,
         int p, q;
         pair_of(round, idx, M2, &p, &q);
         if (q >= (int)m) continue;
-        float* ap = A + (uint64_t)p * la;
-        float* aq = A + (uint64_t)q * la;
-        float al = 0.f, be = 0.f, ga = 0.f;
+        T* ap = A + (uint64_t)p * la;
+        T* aq = A + (uint64_t)q * la;
+        T al = 0, be = 0, ga = 0;
         for (int r = lane; r < la; r += 32) {
-          const float x = ap[r], y = aq[r];
+          const T x = ap[r], y = aq[r];
           al += x * x;
           be += y * y;
           ga += x * y;
         }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        if (al > 0.f && be > 0.f && fabsf(ga) > thresh * sqrtf(al * be)) {
-          const float zeta = (be - al) / (2.f * ga);
-          const float t = copysignf(1.f, zeta) /
-                          (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-          const float c = 1.f / sqrtf(1.f + t * t);
-          const float s = c * t;
+        al = warp_sum_t(al);
+        be = warp_sum_t(be);
+        ga = warp_sum_t(ga);
+        if (al > T(0) && be > T(0) && fabs(ga) > thresh * sqrt(al * be)) {
+          const T zeta = (be - al) / (T(2) * ga);
+          const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          const T c = T(1) / sqrt(T(1) + t * t);
+          const T sn = c * t;
           for (int r = lane; r < la; r += 32) {
-            const float x = ap[r], y = aq[r];
-            ap[r] = c * x - s * y;
-            aq[r] = s * x + c * y;
+            const T x = ap[r], y = aq[r];
+            ap[r] = c * x - sn * y;
+            aq[r] = sn * x + c * y;
           }
-          float* jp = J + (uint64_t)p * m;
-          float* jq = J + (uint64_t)q * m;
+          T* jp = J + (uint64_t)p * m;
+          T* jq = J + (uint64_t)q * m;
           for (int r = lane; r < (int)m; r += 32) {
-            const float x = jp[r], y = jq[r];
-            jp[r] = c * x - s * y;
-            jq[r] = s * x + c * y;
+            const T x = jp[r], y = jq[r];
+            jp[r] = c * x - sn * y;
+            jq[r] = sn * x + c * y;
           }
           if (lane == 0) rotated = 1;
         }
@@ -105,30 +117,34 @@ k_jacobi(const float* __restrict__ Bf, uint32_t m, float* __restrict__ Ub,
   }
 
   // singular values, descending order (ties by index), vectors
-  float* sig = use_smem ? (J + (uint64_t)m * m) : (J + (uint64_t)m * m);
   for (uint32_t i = wid; i < m; i += nw) {
-    const float* ai = A + (uint64_t)i * la;
-    float t = 0.f;
+    const T* ai = A + (uint64_t)i * la;
+    T t = 0;
     for (int r = lane; r < la; r += 32) t += ai[r] * ai[r];
-    t = warp_sum(t);
-    if (lane == 0) sig[i] = sqrtf(t);
+    t = warp_sum_t(t);
+    if (lane == 0) sig[i] = sqrt(t);
   }
   __syncthreads();
   for (uint32_t i = wid; i < m; i += nw) {
-    const float si = sig[i];
+    const T si = sig[i];
     int rank = 0;
     for (uint32_t jj = lane; jj < m; jj += 32) {
-      const float sj = sig[jj];
+      const T sj = sig[jj];
       rank += (sj > si || (sj == si && jj < i)) ? 1 : 0;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rank += __shfl_xor_sync(0xffffffffu, rank, o);
-    if (lane == 0) Sb[rank] = si;
-    const float* ji = J + (uint64_t)i * m;
-    for (uint32_t r = lane; r < m; r += 32) Ub[r + (uint64_t)rank * m] = ji[r];
-    const float* ai = A + (uint64_t)i * la;
-    const float inv = si > 0.f ? 1.f / si : 0.f;
-    for (int r = lane; r < la; r += 32) Vbt[rank + (uint64_t)r * m] = ai[r] * inv;
+    const T* ji = J + (uint64_t)i * m;
+    if (lane == 0) {
+      Sb[rank] = (float)si;
+      if (sb64) sb64[rank] = (double)si;
+      if (ub_last) ub_last[rank] = (double)ji[m - 1];
+    }
+    for (uint32_t r = lane; r < m; r += 32) Ub[r + (uint64_t)rank * m] = (float)ji[r];
+    const T* ai = A + (uint64_t)i * la;
+    const T inv = si > T(0) ? T(1) / si : T(0);
+    for (int r = lane; r < la; r += 32)
+      Vbt[rank + (uint64_t)r * m] = (float)(ai[r] * inv);
   }
   if (threadIdx.x == 0 && info) {
     info[0] = sweep;
@@ -138,11 +154,13 @@ k_jacobi(const float* __restrict__ Bf, uint32_t m, float* __restrict__ Ub,
 
 __global__ void __launch_bounds__(256)
 k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
+                const double* __restrict__ ub_last, const double* __restrict__ sb64,
                 uint32_t m, uint32_t k, float* __restrict__ rem, uint32_t g,
                 float tol, float* __restrict__ smax, uint32_t kc,
-                double* __restrict__ B, RestartStatus* __restrict__ st) {
+                double* __restrict__ B, RestartStatus* __restrict__ st,
+                float* __restrict__ ratios) {
   __shared__ double red[8];
-  __shared__ float rn_s;
+  __shared__ double rn_s;
   __shared__ int conv_s, kc_s;
   double t = 0.0;
   for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) t += (double)rem[c] * rem[c];
@@ -152,13 +170,16 @@ k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < 8; ++w) s += red[w];
-    const float rn = (float)sqrt(s);  // remainder_norm, pca.pyx:1181
+    const double rn = sqrt(s);            // remainder_norm, pca.pyx:1181
     const float S = fmaxf(Sb[0], *smax);  // pca.pyx:1187
     *smax = S;
     uint32_t nconv = 0;
-    for (uint32_t i = 0; i < k; ++i) {
-      const float residual = rn * Ub[(m - 1) + (uint64_t)i * m];  // pca.pyx:1192
-      nconv += fabsf(residual) < tol * S ? 1u : 0u;
+    for (uint32_t i = 0; i < k; ++i) {    // pca.pyx:1190-1193
+      const double u = ub_last ? ub_last[i] : (double)Ub[(m - 1) + (uint64_t)i * m];
+      const double residual = fabs(rn * u);
+      const double bound = (double)tol * (double)S;
+      nconv += residual < bound ? 1u : 0u;
+      if (ratios) ratios[i] = (float)(residual / bound);
     }
     const int conv = nconv == k;
     uint32_t kc_new = max(kc, k + nconv);
@@ -166,63 +187,90 @@ k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
     st->converged = conv;
     st->num_converged = (int)nconv;
     st->k_current = (int)kc_new;
-    st->remainder_norm = rn;
+    st->remainder_norm = (float)rn;
     st->smax = S;
     rn_s = rn;
     conv_s = conv;
     kc_s = (int)kc_new;
   }
   __syncthreads();
-  const float rn = rn_s;
-  for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) rem[c] /= rn;  // :1182-1183
+  const float rnf = (float)rn_s;
+  for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) rem[c] /= rnf;  // :1182-1183
   if (!conv_s) {
     const uint32_t kcn = (uint32_t)kc_s;
     const uint64_t total = (uint64_t)m * (m + 1);
     for (uint64_t t2 = threadIdx.x; t2 < total; t2 += blockDim.x) B[t2] = 0.0;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < kcn; i += blockDim.x) {  // :1227-1231
-      B[i + (uint64_t)i * m] = (double)Sb[i];
-      B[i + (uint64_t)kcn * m] = (double)(rn * Ub[(m - 1) + (uint64_t)i * m]);
+      const double si = sb64 ? sb64[i] : (double)Sb[i];
+      const double u = ub_last ? ub_last[i] : (double)Ub[(m - 1) + (uint64_t)i * m];
+      B[i + (uint64_t)i * m] = si;
+      B[i + (uint64_t)kcn * m] = rn_s * u;
     }
   }
 }
 
-}  // namespace
-
-size_t jacobi_smem_bytes(uint32_t m) {
-  return ((size_t)m * (m + 1) + (size_t)m * m + m) * sizeof(float);
+__global__ void k_f2d(const float* __restrict__ a, uint64_t n, double* __restrict__ b) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
 }
 
-size_t jacobi_global_floats(uint32_t m) {
-  return (size_t)m * (m + 1) + (size_t)m * m + m;
+}  // namespace
+
+int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s) {
+  k_f2d<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(a, n, b);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+size_t jacobi_smem_bytes(uint32_t m, bool fp64) {
+  return ((size_t)m * (m + 1) + (size_t)m * m + m) * (fp64 ? 8 : 4);
+}
+
+size_t jacobi_global_bytes(uint32_t m, bool fp64) {
+  return jacobi_smem_bytes(m, fp64);
 }
 
 float jacobi_threshold(uint32_t m) {
   return std::max(1e-6f, 2.4e-7f * std::sqrt((float)(m + 1)));
 }
 
-int launch_jacobi_svd(const float* Bf, uint32_t m, float* Ub, float* Sb,
-                      float* Vbt, float* gwork, int* info, cudaStream_t s) {
-  const size_t smem = jacobi_smem_bytes(m);
+int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
+                      float* Sb, float* Vbt, double* ub_last, double* sb64,
+                      void* gwork, int* info, cudaStream_t s) {
+  const bool fp64 = Bd != nullptr;
+  const size_t smem = jacobi_smem_bytes(m, fp64);
   const bool use_smem = smem <= 220 * 1024;
   BGPU_REQUIRE(use_smem || gwork, BGPU_ERR_INVALID,
                "small SVD of this size needs a global workspace");
-  if (use_smem && smem > 48 * 1024)
-    BGPU_CUDA(cudaFuncSetAttribute(k_jacobi,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  k_jacobi<<<1, 1024, use_smem ? smem : 0, s>>>(Bf, m, Ub, Sb, Vbt, gwork,
-                                                use_smem ? 1 : 0, 40,
-                                                jacobi_threshold(m), info);
+  if (fp64) {
+    if (use_smem && smem > 48 * 1024)
+      BGPU_CUDA(cudaFuncSetAttribute(k_jacobi<double>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_jacobi<double><<<1, 1024, use_smem ? smem : 0, s>>>(
+        Bd, m, Ub, Sb, Vbt, ub_last, sb64, (double*)gwork, use_smem ? 1 : 0, 40,
+        1e-13, info);
+  } else {
+    if (use_smem && smem > 48 * 1024)
+      BGPU_CUDA(cudaFuncSetAttribute(k_jacobi<float>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_jacobi<float><<<1, 1024, use_smem ? smem : 0, s>>>(
+        Bf, m, Ub, Sb, Vbt, ub_last, sb64, (float*)gwork, use_smem ? 1 : 0, 40,
+        jacobi_threshold(m), info);
+  }
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
 
-int launch_restart_check(const float* Ub, const float* Sb, uint32_t m,
-                         uint32_t k, float* rem, uint32_t g, float tol,
-                         float* smax, uint32_t kc, double* B,
-                         RestartStatus* st, cudaStream_t s) {
-  k_restart_check<<<1, 256, 0, s>>>(Ub, Sb, m, k, rem, g, tol, smax, kc, B, st);
+int launch_restart_check(const float* Ub, const float* Sb, const double* ub_last,
+                         const double* sb64, uint32_t m, uint32_t k, float* rem,
+                         uint32_t g, float tol, float* smax, uint32_t kc,
+                         double* B, RestartStatus* st, float* ratios,
+                         cudaStream_t s) {
+  k_restart_check<<<1, 256, 0, s>>>(Ub, Sb, ub_last, sb64, m, k, rem, g, tol,
+                                    smax, kc, B, st, ratios);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -236,10 +284,19 @@ extern "C" int bgpu_small_svd(const float* B, uint32_t m, float* Ub, float* Sb,
   BGPU_REQUIRE(B && Ub && Sb && Vbt && m >= 1, BGPU_ERR_INVALID,
                "bad small-SVD arguments");
   cudaStream_t s = (cudaStream_t)stream;
-  float* gwork = nullptr;
-  if (jacobi_smem_bytes(m) > 220 * 1024)
-    BGPU_CUDA(cudaMallocAsync((void**)&gwork, jacobi_global_floats(m) * 4, s));
-  int rc = launch_jacobi_svd(B, m, Ub, Sb, Vbt, gwork, nullptr, s);
+  // FP64 Jacobi on a double copy of B (the solver's own precision).
+  const size_t cnt = (size_t)m * (m + 1);
+  double* Bd = nullptr;
+  void* gwork = nullptr;
+  BGPU_CUDA(cudaMallocAsync((void**)&Bd, cnt * 8, s));
+  if (jacobi_smem_bytes(m, true) > 220 * 1024)
+    BGPU_CUDA(cudaMallocAsync(&gwork, jacobi_global_bytes(m, true), s));
+  int rc = launch_float_to_double(B, cnt, Bd, s);
+  if (rc == BGPU_OK)
+    rc = launch_jacobi_svd(nullptr, Bd, m, Ub, Sb, Vbt, nullptr, nullptr, gwork,
+                           nullptr, s);
+  cudaFreeAsync(Bd, s);
   if (gwork) cudaFreeAsync(gwork, s);
+  if (rc == BGPU_OK) BGPU_CUDA(cudaStreamSynchronize(s));
   return rc;
 }

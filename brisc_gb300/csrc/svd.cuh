@@ -14,22 +14,30 @@ struct RestartStatus {
   int pad[3];
 };
 
-size_t jacobi_smem_bytes(uint32_t m);
-size_t jacobi_global_floats(uint32_t m);
+size_t jacobi_smem_bytes(uint32_t m, bool fp64);
+size_t jacobi_global_bytes(uint32_t m, bool fp64);
 float jacobi_threshold(uint32_t m);
+int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s);
 
-// Bf: m x (m+1) column-major. Ub m x m, Sb m, Vbt m x (m+1), column-major.
-// gwork: jacobi_global_floats(m) floats when the matrices do not fit in shared
-// memory (m > ~170); info (2 ints: sweeps, converged) may be null.
-int launch_jacobi_svd(const float* Bf, uint32_t m, float* Ub, float* Sb,
-                      float* Vbt, float* gwork, int* info, cudaStream_t s);
+// One-sided Jacobi SVD of B (m x (m+1), column-major), in FP64 when Bd is
+// given (Bf ignored) or FP32 from Bf. Outputs float Ub (m x m), Sb (m), Vbt
+// (m x (m+1)), column-major; optionally the FP64 last row of Ub (ub_last, m)
+// and FP64 singular values (sb64, m). gwork: jacobi_global_bytes(m, fp64)
+// bytes when the matrices do not fit in shared memory; info (2 ints: sweeps,
+// converged) may be null.
+int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
+                      float* Sb, float* Vbt, double* ub_last, double* sb64,
+                      void* gwork, int* info, cudaStream_t s);
 
 // Normalises rem, updates Smax, counts converged Ritz values, picks the next
 // k_current and (when not converged) rebuilds B as diag(Sb) plus the residual
-// column, exactly as brisc/pca.pyx:1180-1231 orders those steps.
-int launch_restart_check(const float* Ub, const float* Sb, uint32_t m,
-                         uint32_t k, float* rem, uint32_t g, float tol,
-                         float* smax, uint32_t kc, double* B,
-                         RestartStatus* st, cudaStream_t s);
+// column, exactly as brisc/pca.pyx:1180-1231 orders those steps. With ub_last
+// and sb64 the residual test and the new B use the FP64 SVD outputs. ratios
+// (k floats, may be null) receives |residual| / (tol * Smax) per value.
+int launch_restart_check(const float* Ub, const float* Sb, const double* ub_last,
+                         const double* sb64, uint32_t m, uint32_t k, float* rem,
+                         uint32_t g, float tol, float* smax, uint32_t kc,
+                         double* B, RestartStatus* st, float* ratios,
+                         cudaStream_t s);
 
 }  // namespace bgpu

@@ -202,7 +202,7 @@ class DeviceMatrix:
               seed: int = 0, chunk_size: int = 1024, *, reorth_passes: int = 2,
               rotation_mode: int = 0, loadings: bool = False, PCs=None,
               use_graphs: bool = False, profile: bool = False,
-              stream=None) -> SolveResult:
+              svd_fp64: bool = False, stream=None) -> SolveResult:
         o = L.SolveOpts()
         L.lib().bgpu_solve_opts_default(C.byref(o))
         o.k, o.subspace_size = int(num_PCs), int(subspace_size)
@@ -210,6 +210,7 @@ class DeviceMatrix:
         o.seed, o.chunk_size = int(seed) & 0xFFFFFFFFFFFFFFFF, int(chunk_size)
         o.reorth_passes, o.rotation_mode = int(reorth_passes), int(rotation_mode)
         o.use_graphs, o.profile = int(use_graphs), int(profile)
+        o.svd_fp64 = int(svd_fp64)
         on_dev = PCs is not None and not isinstance(PCs, np.ndarray)
         if PCs is None:
             PCs = np.empty((self.num_cells, num_PCs), dtype=np.float32)

@@ -136,6 +136,8 @@ typedef struct bgpu_solve_opts {
   int use_graphs;            /* replay each Lanczos step from a CUDA graph       */
   int profile;               /* time the sparse products and the small SVD with
                                 CUDA events (fills the *_seconds fields)         */
+  int svd_fp64;              /* small SVD in FP64 (1) or FP32 (0); B and the
+                                convergence test are FP64 either way            */
 } bgpu_solve_opts;
 
 typedef struct bgpu_solve_info {
