@@ -145,8 +145,7 @@ k_finish_norm(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride
 }
 
 __global__ void __launch_bounds__(1024)
-k_vstep(const float* __restrict__ zpart, uint32_t num_panels,
-        const float* __restrict__ sd, float* __restrict__ V, uint64_t ldv,
+k_vstep(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
         uint32_t g, uint32_t j, uint32_t m, const float* __restrict__ scal,
         double* __restrict__ B, float* __restrict__ rem, int passes) {
   extern __shared__ float dots[];  // m floats
@@ -155,12 +154,8 @@ k_vstep(const float* __restrict__ zpart, uint32_t num_panels,
   const float alpha = scal[0];
   float* z = (j + 1 < m) ? V + (uint64_t)(j + 1) * ldv : rem;
   const float* vj = V + (uint64_t)j * ldv;
-  for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) {
-    float t = 0.f;
-    for (uint32_t p = 0; p < num_panels; ++p) t += zpart[(uint64_t)p * g + c];
-    t = t / sd[c];           // pca.pyx:510-511
-    z[c] = t - alpha * vj[c];  // pca.pyx:1104-1105
-  }
+  for (uint32_t c = threadIdx.x; c < g; c += blockDim.x)
+    z[c] = zin[c] - alpha * vj[c];  // pca.pyx:1104-1105
   __syncthreads();
   for (int pass = 0; pass < passes; ++pass) {
     for (uint32_t col = wid; col <= j; col += 32) {
@@ -328,12 +323,11 @@ int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
   return BGPU_OK;
 }
 
-int launch_vstep(const float* zpart, uint32_t num_panels, const float* sd,
-                 float* V, uint64_t ldv, uint32_t g, uint32_t j, uint32_t m,
-                 const float* scal, double* B, float* rem, int passes,
-                 cudaStream_t s) {
+int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
+                 uint32_t j, uint32_t m, const float* scal, double* B,
+                 float* rem, int passes, cudaStream_t s) {
   k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(
-      zpart, num_panels, sd, V, ldv, g, j, m, scal, B, rem, passes);
+      z, V, ldv, g, j, m, scal, B, rem, passes);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -32,13 +32,13 @@ int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
                        double* B, uint32_t m, uint32_t j, float* scal,
                        cudaStream_t s);
 
-// V-side half step (pca.pyx:1103-1171): z = (sum_p zpart[p]) / sd - alpha V[:, j],
-// `passes` rounds of classical Gram-Schmidt against V[:, :j+1]; then either
-// V[:, j+1] = z / beta, B[j, j+1] = beta (j < m-1) or rem = z (j == m-1).
-int launch_vstep(const float* zpart, uint32_t num_panels, const float* sd,
-                 float* V, uint64_t ldv, uint32_t g, uint32_t j, uint32_t m,
-                 const float* scal, double* B, float* rem, int passes,
-                 cudaStream_t s);
+// V-side half step (pca.pyx:1103-1171): given z = (X^T u) / sd, forms
+// z - alpha V[:, j], runs `passes` rounds of classical Gram-Schmidt against
+// V[:, :j+1]; then either V[:, j+1] = z / beta, B[j, j+1] = beta (j < m-1)
+// or rem = z (j == m-1).
+int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
+                 uint32_t j, uint32_t m, const float* scal, double* B,
+                 float* rem, int passes, cudaStream_t s);
 
 // C = A . Bop (tall-skinny): A is rows x K column-major (lda), Bop(i, c) =
 // Bp[i * bsr + c * bsc] (K x ncols), optional per-column scale cs[c] applied

@@ -137,8 +137,9 @@ struct Solver {
   cudaStream_t s;
   float tol;
 
-  Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, rem, sd, Bf, Ub, Sb, Vbt,
-      svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last, sb64, ratios;
+  Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
+      Vbt, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last, sb64, ratios,
+      derr;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
   PinnedStatus hst;
@@ -209,6 +210,8 @@ struct Solver {
     BGPU_TRY(balloc(part, nb * ps * 4, true, s));
     BGPU_TRY(balloc(coef, 2 * (size_t)ps * 4, true, s));
     BGPU_TRY(balloc(zpart, (size_t)X.num_panels * g * 4, true, s));
+    BGPU_TRY(balloc(zvec, ldv * 4, true, s));
+    BGPU_TRY(balloc(derr, 16, true, s));
     BGPU_TRY(balloc(rem, ldv * 4, true, s));
     BGPU_TRY(balloc(sd, ldv * 4, true, s));
     BGPU_TRY(balloc(Bf, (size_t)m * (m + 1) * 4, true, s));
@@ -241,7 +244,11 @@ struct Solver {
     float* coef2 = coefp + ps;
     float* Up = U.as<float>();
     BGPU_TRY(ev_begin(0));
-    BGPU_TRY(launch_matvec(X, Vcol(j), sd.as<float>(), y0p, s));
+    if (X.stream_ok && X.impl == 0)
+      BGPU_TRY(launch_matvec_stream(X, Vcol(j), sd.as<float>(), y0p,
+                                    derr.as<int>(), s));
+    else
+      BGPU_TRY(launch_matvec(X, Vcol(j), sd.as<float>(), y0p, s));
     BGPU_TRY(ev_end());
     launches += 1;
     const double col = (double)n * 4.0;
@@ -282,13 +289,19 @@ struct Solver {
     BGPU_TRY(launch_finish_norm(partp, nb, ps, B.as<double>(), m, j, scalp, s));
     BGPU_TRY(ev_end());
     BGPU_TRY(ev_begin(1));
-    BGPU_TRY(launch_rmatvec_partials(X, yfin, scalp + 1, Ucol(j),
-                                     zpart.as<float>(), s));
+    if (X.stream_ok && X.impl == 0)
+      BGPU_TRY(launch_rmatvec_stream(X, yfin, scalp + 1, Ucol(j),
+                                     zpart.as<float>(), derr.as<int>(), s));
+    else
+      BGPU_TRY(launch_rmatvec_partials(X, yfin, scalp + 1, Ucol(j),
+                                       zpart.as<float>(), s));
+    BGPU_TRY(launch_reduce_panels_t(X, zpart.as<float>(), sd.as<float>(),
+                                    zvec.as<float>(), s));
+    launches += 1;
     BGPU_TRY(ev_end());
     BGPU_TRY(ev_begin(4));
-    BGPU_TRY(launch_vstep(zpart.as<float>(), X.num_panels, sd.as<float>(),
-                          V.as<float>(), ldv, g, j, m, scalp, B.as<double>(),
-                          rem.as<float>(), passes, s));
+    BGPU_TRY(launch_vstep(zvec.as<float>(), V.as<float>(), ldv, g, j, m, scalp,
+                          B.as<double>(), rem.as<float>(), passes, s));
     BGPU_TRY(ev_end());
     launches += 3;
     reorth_bytes += (double)(j + 1) * g * 4.0 * 2 * passes;
@@ -378,6 +391,13 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
                               cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaStreamSynchronize(s));
     BGPU_TRY(S.ev_collect());
+    {
+      int derr = 0;
+      BGPU_CUDA(cudaMemcpy(&derr, S.derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+      BGPU_REQUIRE(derr == 0, BGPU_ERR_DEVICE,
+                   "a bulk copy into shared memory did not complete within its "
+                   "time limit (device error word " + std::to_string(derr) + ")");
+    }
     last = *S.hst.h;
     if (S.trace) {
       std::vector<float> rat(k);
@@ -495,6 +515,13 @@ static void choose_shapes(Matrix& m) {
   m.spmv_group = G;
   m.spmv_blocks = num_sms() * 8;
   m.rmat_colgroup = m.g <= 512 ? 64 : 256;
+  // BGPU_SPMV_LEGACY=1 selects the register-vector products (for A/B study)
+  const char* leg = std::getenv("BGPU_SPMV_LEGACY");
+  m.impl = (leg && leg[0] == '1') ? 1 : 0;
+  const char* rb = std::getenv("BGPU_SPMV_R");
+  if (rb) m.spmv_rows_per_batch = std::atoi(rb) >= 4 ? 4 : 2;
+  const char* gb = std::getenv("BGPU_RMAT_R");
+  if (gb) m.rmat_genes_per_batch = std::atoi(gb) >= 8 ? 8 : 4;
 }
 
 extern "C" int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* d,
@@ -530,7 +557,17 @@ extern "C" int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes) {
 extern "C" int bgpu_matrix_matvec(const bgpu_matrix* mat, const float* v,
                                   const float* sd, float* y, void* stream) {
   BGPU_REQUIRE(mat && v && y, BGPU_ERR_INVALID, "NULL argument");
-  return launch_matvec(mat->m, v, sd, y, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!(mat->m.stream_ok && mat->m.impl == 0))
+    return launch_matvec(mat->m, v, sd, y, s);
+  Buf err;
+  BGPU_TRY(balloc(err, 16, true, s));
+  BGPU_TRY(launch_matvec_stream(mat->m, v, sd, y, err.as<int>(), s));
+  int h = 0;
+  BGPU_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  BGPU_REQUIRE(h == 0, BGPU_ERR_DEVICE, "bulk copy wait timed out");
+  return BGPU_OK;
 }
 
 extern "C" int bgpu_matrix_rmatvec(const bgpu_matrix* mat, const float* u,
@@ -539,9 +576,19 @@ extern "C" int bgpu_matrix_rmatvec(const bgpu_matrix* mat, const float* u,
   cudaStream_t s = (cudaStream_t)stream;
   Buf part;
   BGPU_TRY(balloc(part, (size_t)mat->m.num_panels * mat->m.g * 4, false, s));
-  BGPU_TRY(launch_rmatvec_partials(mat->m, u, nullptr, nullptr, part.as<float>(), s));
-  BGPU_TRY(launch_reduce_panels(mat->m, part.as<float>(), sd, z, s));
+  Buf err;
+  BGPU_TRY(balloc(err, 16, true, s));
+  if (mat->m.stream_ok && mat->m.impl == 0)
+    BGPU_TRY(launch_rmatvec_stream(mat->m, u, nullptr, nullptr, part.as<float>(),
+                                   err.as<int>(), s));
+  else
+    BGPU_TRY(launch_rmatvec_partials(mat->m, u, nullptr, nullptr,
+                                     part.as<float>(), s));
+  BGPU_TRY(launch_reduce_panels_t(mat->m, part.as<float>(), sd, z, s));
+  int h = 0;
+  BGPU_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
   BGPU_CUDA(cudaStreamSynchronize(s));
+  BGPU_REQUIRE(h == 0, BGPU_ERR_DEVICE, "bulk copy wait timed out");
   return BGPU_OK;
 }
 

@@ -305,11 +305,11 @@ uint32_t choose_pshift(uint64_t n, uint32_t requested) {
     while ((1u << p) < requested) ++p;
     return p;
   }
-  // Enough panels that panels x gene groups fills the GPU several times, with
-  // the per-panel staging (8 bytes per row) at most 64 KB of shared memory.
-  uint32_t p = 13;
-  while (p > 10 && (n >> p) < 40) --p;
-  return p;
+  // 1024-row panels: the streaming X^T.u stages u and an 8-count table per
+  // panel row in shared memory (36 KB), keeps two CTAs per SM, and a panel's
+  // local row fits the 16-bit field of the packed entry.
+  (void)n;
+  return 10;
 }
 
 }  // namespace
@@ -402,7 +402,10 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
   BGPU_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), s));
 
   // Persistent arrays.
-  BGPU_TRY(dev_alloc(&m->rowptr, m->n + 1, &m->bytes));
+  // rowptr, isf and post carry 4 padding entries: the streaming X.v copies
+  // 16-byte-aligned slices of them that may end past the last row.
+  BGPU_TRY(dev_alloc(&m->rowptr, m->n + 5, &m->bytes));
+  BGPU_CUDA(cudaMemsetAsync(m->rowptr, 0, (m->n + 5) * 8, s));
   if (m->mode == kFloat) {
     BGPU_TRY(dev_alloc(&m->csr_val, m->nnz_alloc, &m->bytes));
     BGPU_TRY(dev_alloc(&m->csr_col, m->nnz_alloc, &m->bytes));
@@ -417,11 +420,13 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     BGPU_TRY(dev_alloc(&m->csc_packed, m->nnz_alloc, &m->bytes));
     BGPU_CUDA(cudaMemsetAsync(m->csr_packed, 0, m->nnz_alloc * 4, s));
     BGPU_CUDA(cudaMemsetAsync(m->csc_packed, 0, m->nnz_alloc * 4, s));
-    BGPU_TRY(dev_alloc(&m->isf, m->n, &m->bytes));
+    BGPU_TRY(dev_alloc(&m->isf, m->n + 4, &m->bytes));
+    BGPU_CUDA(cudaMemsetAsync(m->isf, 0, (m->n + 4) * 4, s));
     k_copy_float<<<grid_for(m->n, 256), 256, 0, s>>>(isf, m->isf, m->n);
     BGPU_CHECK_LAUNCH();
     if (m->norm_method == BGPU_NORM_PFLOG1PPF) {
-      BGPU_TRY(dev_alloc(&m->post, m->n, &m->bytes));
+      BGPU_TRY(dev_alloc(&m->post, m->n + 4, &m->bytes));
+      BGPU_CUDA(cudaMemsetAsync(m->post, 0, (m->n + 4) * 4, s));
       k_copy_float<<<grid_for(m->n, 256), 256, 0, s>>>(post, m->post, m->n);
       BGPU_CHECK_LAUNCH();
     }
@@ -447,6 +452,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     BGPU_TRY(pack_by_value<int32_t>(m, d->value_type, idx, val, d_err, s));
 
   // Panel-relative offsets fit in int32 if every panel holds < 2^31 entries.
+  std::vector<int64_t> panel_rp;
   {
     std::vector<int64_t> rp(m->num_panels + 1);
     DevBuf t_rp;
@@ -474,6 +480,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     for (uint32_t p = 0; p < m->num_panels; ++p)
       BGPU_REQUIRE(rp[p + 1] - rp[p] < (int64_t)INT32_MAX, BGPU_ERR_UNSUPPORTED,
                    "a row panel holds >= 2^31 entries; use a smaller panel_rows");
+    panel_rp.swap(rp);
   }
 
   // Transposed copy.
@@ -500,6 +507,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
         m->pshift, cnt, m->csc_packed, nullptr, nullptr);
   }
   BGPU_CHECK_LAUNCH();
+  BGPU_TRY(build_stream_tiles(m, panel_rp, s, &m->bytes));
   BGPU_CUDA(cudaStreamSynchronize(s));  // temporaries are freed on return
   return BGPU_OK;
 }
@@ -507,7 +515,8 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
 void matrix_free(Matrix* m) {
   void* ptrs[] = {m->rowptr, m->csr_packed, m->csr_val, m->csr_col,
                   m->colptr, m->csc_packed, m->csc_val, m->csc_row,
-                  m->isf,    m->post,       m->sd};
+                  m->isf,    m->post,       m->sd,      m->rtab_r,
+                  m->rtab_c};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   *m = Matrix();

@@ -19,11 +19,17 @@
 // entries starting at a multiple of 4 stays inside the allocation.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace bgpu {
 
 enum MatrixMode { kCounts = 0, kFloat = 1 };
+
+// Per-cell table of normalised values for small counts:
+// tab[c] = log1pf(c * isf) for 1 <= c < 16 and tab[0] = isf (for larger counts).
+constexpr int kCountTab = 16;
 
 struct Matrix {
   uint64_t n = 0;
@@ -48,15 +54,23 @@ struct Matrix {
 
   float* isf = nullptr;
   float* post = nullptr;
+  float* rtab_r = nullptr;  // [cell][kCountTab] (X.v)
+  float* rtab_c = nullptr;  // [panel][kCountTab][P] (X^T.u)
 
   float* sd = nullptr;  // cached clipped gene std (computed on first use)
   int device = 0;
   uint64_t bytes = 0;
 
   // Autotuned SpMV shapes (chosen at creation from the nnz-per-row histogram).
-  int spmv_group = 16;     // lanes per row
-  int spmv_blocks = 0;     // CTAs
-  int rmat_colgroup = 256; // genes per CTA in the transposed product
+  int spmv_group = 16;     // lanes per row (register-vector kernel)
+  int spmv_blocks = 0;     // CTAs (register-vector kernel)
+  int rmat_colgroup = 256; // genes per CTA (register-vector transposed product)
+
+  // Table-driven products (stream.cu) for the counts layout.
+  bool stream_ok = false;  // count tables built; the table-driven kernels apply
+  int impl = 0;            // 0 = table-driven kernels, 1 = register-vector kernels
+  int spmv_rows_per_batch = 2;   // X.v rows per half-warp batch (2 or 4)
+  int rmat_genes_per_batch = 4;  // X^T.u gene segments per half-warp batch (4 or 8)
 };
 
 // Per-launch views passed by value to kernels.
@@ -69,6 +83,7 @@ struct CsrView {
   const float* post;
   uint64_t n;
   uint32_t g;
+  const float* rtab;  // [cell][kCountTab], counts mode
 };
 struct CscView {
   const int64_t* rowptr;
@@ -82,16 +97,17 @@ struct CscView {
   uint32_t g;
   uint32_t pshift;
   uint32_t num_panels;
+  const float* rtab;  // [panel][kCountTab][P], counts mode
 };
 
 inline CsrView csr_view(const Matrix& m) {
-  return CsrView{m.rowptr, m.csr_packed, m.csr_val, m.csr_col,
-                 m.isf,    m.post,       m.n,       m.g};
+  return CsrView{m.rowptr, m.csr_packed, m.csr_val, m.csr_col, m.isf,
+                 m.post,   m.n,          m.g,       m.rtab_r};
 }
 inline CscView csc_view(const Matrix& m) {
   return CscView{m.rowptr, m.colptr, m.csc_packed, m.csc_val, m.csc_row,
                  m.isf,    m.post,   m.n,          m.g,       m.pshift,
-                 m.num_panels};
+                 m.num_panels, m.rtab_c};
 }
 
 // layout.cu
@@ -101,16 +117,28 @@ void matrix_free(Matrix* m);
 // spmv.cu: raw products on the layout (device pointers)
 int launch_matvec(const Matrix& m, const float* v, const float* sd, float* y,
                   cudaStream_t s);
-// X^T u: per-panel partials (num_panels x g) then a fixed-order reduction.
-// `u_scale_dev` (device scalar, may be null) multiplies u on load; when
-// `u_out` is non-null the normalised u is also written there.
+// X^T u: per-panel partials (gene-major: partT[gene * num_panels + panel]),
+// reduced in panel order by launch_reduce_panels_t. `u_scale_dev` (device
+// scalar, may be null) multiplies u on load; when `u_out` is non-null the
+// scaled u is also written there.
 int launch_rmatvec_partials(const Matrix& m, const float* u,
                             const float* u_scale_dev, float* u_out,
                             float* partials, cudaStream_t s);
-int launch_reduce_panels(const Matrix& m, const float* partials,
-                         const float* sd, float* z, cudaStream_t s);
 int launch_gene_stddev(const Matrix& m, double* partials, float* sd,
                        cudaStream_t s);
+
+// stream.cu: table-driven products for the counts layout (partials of X^T u
+// are gene-major: partT[gene * num_panels + panel]). build_stream_tiles builds
+// the per-cell count tables when the layout allows the table-driven kernels.
+bool stream_supported(const Matrix& m);
+int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
+                       cudaStream_t s, uint64_t* bytes_acc);
+int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
+                         float* y, int* err, cudaStream_t s);
+int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
+                          float* u_out, float* partT, int* err, cudaStream_t s);
+int launch_reduce_panels_t(const Matrix& m, const float* partT, const float* sd,
+                           float* z, cudaStream_t s);
 
 // Bytes of the algorithmic traffic of one X.v / X^T.u launch (used for the
 // roofline figure). Counts what the chosen layout must stream.

@@ -9,8 +9,10 @@
 //          (row panel, gene group). The panel's u and size factors are staged
 //          in shared memory, so the per-entry gathers hit shared memory instead
 //          of L2; one warp reduces one gene's segment (a warp-segmented
-//          reduction, no atomics) into a per-panel partial; a second pass adds
-//          the partials of all panels in panel order.
+//          reduction, no atomics) into a per-panel partial (gene-major
+//          layout); a second pass adds the partials of all panels in panel
+//          order. These register-vector kernels serve layouts outside the
+//          streaming kernels' limits (stream.cu).
 //  gene sd (brisc/pca.pyx:51-103 clipped_stddev_csc): same panel traversal,
 //          FP64 sums.
 #include <algorithm>
@@ -141,20 +143,8 @@ k_rmat_partials(CscView X, const float* __restrict__ u,
       }
     }
     acc = warp_sum(acc);
-    if (lane == 0) partials[(uint64_t)p * X.g + c] = acc;
+    if (lane == 0) partials[(uint64_t)c * X.num_panels + p] = acc;
   }
-}
-
-// z[c] = (sum over panels, in panel order, of partials[p][c]) / sd[c]
-__global__ void k_reduce_panels(const float* __restrict__ partials,
-                                uint32_t num_panels, uint32_t g,
-                                const float* __restrict__ sd,
-                                float* __restrict__ z) {
-  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g) return;
-  float t = 0.f;
-  for (uint32_t p = 0; p < num_panels; ++p) t += partials[(uint64_t)p * g + c];
-  z[c] = sd ? t / sd[c] : t;  // pca.pyx:510-511
 }
 
 template <int MODE>
@@ -312,14 +302,6 @@ int launch_rmatvec_partials(const Matrix& m, const float* u,
     k_rmat_partials<kFloat><<<grid, 256, smem, s>>>(X, u, u_scale_dev, u_out,
                                                     partials, cg);
   }
-  BGPU_CHECK_LAUNCH();
-  return BGPU_OK;
-}
-
-int launch_reduce_panels(const Matrix& m, const float* partials, const float* sd,
-                         float* z, cudaStream_t s) {
-  k_reduce_panels<<<(unsigned)ceil_div(m.g, 256), 256, 0, s>>>(
-      partials, m.num_panels, m.g, sd, z);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

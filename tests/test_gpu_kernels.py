@@ -84,6 +84,8 @@ def test_size_factors_and_normalize(cuda, golden, method, tag):
 def _mat(n=6000, g=700, density=0.05, seed=4, empty_rows=True):
     c = nb_counts(n, g, seed=seed, density=density, workers=1)
     X = c.to_scipy()
+    X.data[::331] = np.minimum(X.data[::331].astype(np.int64) * 97 + 16,
+                               65535).astype(X.data.dtype)  # counts beyond the tables
     if empty_rows:  # a few cells with no counts, and the last cell empty
         X = X.tolil()
         for r in (3, 17, X.shape[0] - 1):
@@ -97,24 +99,35 @@ def _mat(n=6000, g=700, density=0.05, seed=4, empty_rows=True):
     return X, isf
 
 
-def _normalized(X, isf):
+def _normalized(X, isf, post=None):
     rows = np.repeat(np.arange(X.shape[0]), np.diff(X.indptr))
     v = np.log1p(X.data.astype(np.float64) * isf[rows].astype(np.float64))
+    if post is not None:
+        v *= post[rows].astype(np.float64)
     return sp.csr_matrix((v, X.indices, X.indptr), shape=X.shape)
 
 
-@pytest.mark.parametrize("mode", ["counts", "float"])
+@pytest.mark.parametrize("mode", ["counts", "counts_post", "float"])
 @pytest.mark.parametrize("itype", [np.int32, np.int64])
-@pytest.mark.parametrize("panel_rows", [0, 1024])
-def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows):
+@pytest.mark.parametrize("panel_rows", [0, 2048])
+@pytest.mark.parametrize("impl", ["stream", "vector"])
+def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows, impl, monkeypatch):
     import torch
+    monkeypatch.setenv("BGPU_SPMV_LEGACY", "1" if impl == "vector" else "0")
     X, isf = _mat()
     n, g = X.shape
-    Xn = _normalized(X, isf)
+    post = None
+    if mode == "counts_post":  # per-cell post-log factors (PFlog1pPF layout)
+        post = np.random.default_rng(1).uniform(0.5, 2.0, n).astype(np.float32)
+    Xn = _normalized(X, isf, post)
     ip, ix = X.indptr.astype(itype), X.indices.astype(itype)
     if mode == "counts":
         M = DeviceMatrix(ip, ix, X.data.astype(np.uint16), n, g, norm="logCP10k",
                          inv_size_factors=isf, panel_rows=panel_rows)
+    elif mode == "counts_post":
+        M = DeviceMatrix(ip, ix, X.data.astype(np.uint16), n, g, norm="PFlog1pPF",
+                         inv_size_factors=isf, post_factors=post,
+                         panel_rows=panel_rows)
     else:
         M = DeviceMatrix(ip, ix, Xn.data.astype(np.float32), n, g,
                          panel_rows=panel_rows)
