@@ -99,6 +99,7 @@ SIGNATURES = {
                             C.POINTER(_i)]),
     "bgpu_start_vector": (_i, [_u64, _u32, _vp]),
     "bgpu_small_svd": (_i, [_vp, _u32, _vp, _vp, _vp, _vp]),
+    "bgpu_small_svd_noalloc": (_i, [_vp, _u32, _vp, _vp, _vp, _vp]),
     "bgpu_size_factors": (_i, [_vp, _i, _vp, _i, _u64, _i, _vp, _vp, _vp, _vp, _vp]),
     "bgpu_normalize_csr": (_i, [_vp, _i, _vp, _i, _u64, _vp, _vp, _vp, _vp]),
     "bgpu_csr_tocsc": (_i, [_u64, _u32, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),

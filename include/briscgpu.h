@@ -201,6 +201,18 @@ BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_hos
 BGPU_API int bgpu_small_svd(const float* B, uint32_t m, float* Ub, float* Sb,
                    float* Vbt, void* stream);
 
+/* The same SVD as bgpu_small_svd, for callers that cannot allocate device
+ * memory: their process gives all of it to its own pool allocator, or they run
+ * in a loop where cudaMalloc/cudaFree would stall the device. No counterpart in
+ * the reference (its sgesdd call allocates host workspace, pca.pyx:514-528).
+ * Allocates nothing: its scratch is a fixed device array inside the library
+ * (about 1.6 MB per GPU that loads it, held until exit). m <= 256, else
+ * BGPU_ERR_INVALID. The first call on each device looks the array up; make it
+ * before any stream capture. Calls share the array: two whose work overlaps on
+ * the GPU race. Returns after the SVD has completed on `stream`. */
+BGPU_API int bgpu_small_svd_noalloc(const float* B, uint32_t m, float* Ub,
+                                    float* Sb, float* Vbt, void* stream);
+
 /* Per-cell normalisation factors (brisc/normalize.pyx:9-268), on the GPU,
  * over a full-gene counts CSR (device pointers). Writes inverse size factors
  * `isf` (num_cells floats) and, for method 2, `post` (num_cells floats).
