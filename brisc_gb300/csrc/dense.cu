@@ -7,7 +7,11 @@
 // fixed xor-shuffle tree, or a sum over fixed 1024-row blocks in block order.
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "dense.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace bgpu {
 
@@ -193,6 +197,84 @@ k_vstep(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
   }
 }
 
+// V-side step on one 8-CTA thread-block cluster: CTA q owns genes
+// [q*slice, (q+1)*slice) and keeps its part of z in shared memory; the
+// Gram-Schmidt dots and the norm are all-reduced through distributed shared
+// memory, every CTA summing the 8 partials in rank order (so all CTAs hold
+// the same bits and the result does not depend on timing).
+constexpr int kVCluster = 8;
+constexpr int kVThreads = 256;
+
+__global__ void __cluster_dims__(kVCluster, 1, 1) __launch_bounds__(kVThreads)
+k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
+                uint32_t g, uint32_t j, uint32_t m, const float* __restrict__ scal,
+                double* __restrict__ B, float* __restrict__ rem, int passes) {
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) float vsm[];
+  const uint32_t slice = (g + kVCluster - 1) / kVCluster;
+  float* zs = vsm;                            // slice
+  float* pd = zs + ((slice + 3) & ~3u);       // 2 x m partial dots (per pass)
+  float* dots = pd + 2 * m;                   // m
+  __shared__ double pn;                       // partial squared norm
+  __shared__ double wred[kVThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t q = cluster.block_rank();
+  const uint32_t c0 = q * slice, c1 = min(g, c0 + slice);
+  const float alpha = scal[0];
+  const float* vj = V + (uint64_t)j * ldv;
+  for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
+    zs[c - c0] = zin[c] - alpha * vj[c];  // pca.pyx:1104-1105
+  __syncthreads();
+  for (int pass = 0; pass < passes; ++pass) {
+    float* pdp = pd + (pass & 1) * m;
+    for (uint32_t col = wid; col <= j; col += kVThreads / 32) {
+      const float* vc = V + (uint64_t)col * ldv;
+      float d = 0.f;
+      for (uint32_t c = c0 + lane; c < c1; c += 32) d += vc[c] * zs[c - c0];
+      d = warp_sum(d);
+      if (lane == 0) pdp[col] = d;
+    }
+    cluster.sync();  // every CTA's partials are visible
+    for (uint32_t col = threadIdx.x; col <= j; col += kVThreads) {
+      float t = 0.f;
+      for (uint32_t r = 0; r < kVCluster; ++r) t += cluster.map_shared_rank(pdp, r)[col];
+      dots[col] = t;
+    }
+    __syncthreads();
+    for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads) {
+      float t = 0.f;
+      for (uint32_t col = 0; col <= j; ++col) t += V[c + (uint64_t)col * ldv] * dots[col];
+      zs[c - c0] -= t;
+    }
+    __syncthreads();
+  }
+  float* out = (j + 1 < m) ? V + (uint64_t)(j + 1) * ldv : rem;
+  if (j + 1 < m) {
+    double ss = 0.0;
+    for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
+      ss += (double)zs[c - c0] * zs[c - c0];
+    ss = warp_sum(ss);
+    if (lane == 0) wred[wid] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kVThreads / 32; ++w) t += wred[w];
+      pn = t;
+    }
+    cluster.sync();
+    double s2 = 0.0;
+    for (uint32_t r = 0; r < kVCluster; ++r) s2 += *cluster.map_shared_rank(&pn, r);
+    double beta = sqrt(s2);
+    if (beta < 1e-8) beta = 1e-8;  // pca.pyx:1165-1166
+    if (q == 0 && threadIdx.x == 0) B[j + (uint64_t)(j + 1) * m] = beta;
+    const float inv = 1.f / (float)beta;
+    for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads) out[c] = zs[c - c0] * inv;
+  } else {
+    for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads) out[c] = zs[c - c0];
+  }
+  cluster.sync();  // no CTA leaves while another may read its shared memory
+}
+
 // Tall-skinny SIMT GEMM: CTA tile 128 rows x 128 columns, K in steps of 16.
 constexpr int BM = 128, BN = 128, BK = 16;
 
@@ -326,8 +408,15 @@ int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
 int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
                  uint32_t j, uint32_t m, const float* scal, double* B,
                  float* rem, int passes, cudaStream_t s) {
-  k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(
-      z, V, ldv, g, j, m, scal, B, rem, passes);
+  const uint32_t slice = (g + kVCluster - 1) / kVCluster;
+  const size_t csm = ((size_t)((slice + 3) & ~3u) + 3ull * m) * sizeof(float);
+  if (csm <= 48 * 1024) {
+    k_vstep_cluster<<<kVCluster, kVThreads, csm, s>>>(z, V, ldv, g, j, m, scal, B,
+                                                     rem, passes);
+  } else {
+    k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(
+        z, V, ldv, g, j, m, scal, B, rem, passes);
+  }
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

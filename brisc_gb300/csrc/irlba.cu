@@ -515,13 +515,16 @@ static void choose_shapes(Matrix& m) {
   m.spmv_group = G;
   m.spmv_blocks = num_sms() * 8;
   m.rmat_colgroup = m.g <= 512 ? 64 : 256;
-  // BGPU_SPMV_LEGACY=1 selects the register-vector products (for A/B study)
-  const char* leg = std::getenv("BGPU_SPMV_LEGACY");
-  m.impl = (leg && leg[0] == '1') ? 1 : 0;
-  const char* rb = std::getenv("BGPU_SPMV_R");
-  if (rb) m.spmv_rows_per_batch = std::atoi(rb) >= 4 ? 4 : 2;
-  const char* gb = std::getenv("BGPU_RMAT_R");
-  if (gb) m.rmat_genes_per_batch = std::atoi(gb) >= 8 ? 8 : 4;
+  // X.v kernel: the segmented stream keeps every lane busy on short rows;
+  // 8 lanes per row amortise their per-row work better on long ones.
+  m.spmv_seg = m.csr_heads && avg < 64.0;
+  // BGPU_SPMV_IMPL = vector | rows | seg overrides the choice (A/B study)
+  if (const char* e = std::getenv("BGPU_SPMV_IMPL")) {
+    const std::string k(e);
+    m.impl = k == "vector" ? 1 : 0;
+    if (k == "rows") m.spmv_seg = false;
+    if (k == "seg") m.spmv_seg = m.csr_heads;
+  }
 }
 
 extern "C" int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* d,

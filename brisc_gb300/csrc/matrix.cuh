@@ -6,9 +6,14 @@
 //                                          [rowptr[p*P], rowptr[(p+1)*P]) in the
 //                                          CSR copy AND in the transposed copy)
 //   kCounts mode (fused normalisation, 4 bytes per stored entry):
-//     csr_packed  uint32[nnz4]            (gene << 16) | count
+//     csr_packed  uint32[nnz4]            (gene << 16) | count; bit 31 flags the
+//                                          first entry of a row when g <= 32768
 //     csc_packed  uint32[nnz4]            (local_row << 16) | count, grouped by
-//                                          row panel, then gene, rows ascending
+//                                          row panel, then gene, rows ascending;
+//                                          bit 31 flags the first entry of each
+//                                          (panel, gene) segment
+//     rtab_c      float32[panels*16*P]    per panel, [count][row] table of
+//                                          log1pf(count * isf) (count 0 -> 0)
 //     isf, post   float32[n]              per-cell factors (post may be null)
 //   kFloat mode (pre-normalised values, 6 bytes per stored entry):
 //     csr_val float32[nnz4], csr_col uint16[nnz4]
@@ -28,7 +33,7 @@ namespace bgpu {
 enum MatrixMode { kCounts = 0, kFloat = 1 };
 
 // Per-cell table of normalised values for small counts:
-// tab[c] = log1pf(c * isf) for 1 <= c < 16 and tab[0] = isf (for larger counts).
+// tab[c] = log1pf(c * isf) for 1 <= c < 16 and tab[0] = 0.
 constexpr int kCountTab = 16;
 
 struct Matrix {
@@ -68,9 +73,10 @@ struct Matrix {
 
   // Table-driven products (stream.cu) for the counts layout.
   bool stream_ok = false;  // count tables built; the table-driven kernels apply
+  bool csr_heads = false;  // CSR words carry row-head flags (segmented X.v)
+  bool spmv_seg = false;   // X.v by the segmented stream (short rows) rather
+                           // than 8 lanes per row
   int impl = 0;            // 0 = table-driven kernels, 1 = register-vector kernels
-  int spmv_rows_per_batch = 2;   // X.v rows per half-warp batch (2 or 4)
-  int rmat_genes_per_batch = 4;  // X^T.u gene segments per half-warp batch (4 or 8)
 };
 
 // Per-launch views passed by value to kernels.

@@ -37,6 +37,8 @@ k_spmv(CsrView X, const float* __restrict__ v, const float* __restrict__ sd,
   const int grp = (threadIdx.x & 31) / G;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  // bit 31 of a stored word flags a row head when genes fit in 15 bits
+  const uint32_t gm = X.g > 32768u ? 0xffffu : 0x7fffu;
   const uint64_t nbatches = ceil_div_dev(X.n, kRowsPerWarp);
   for (uint64_t bt = warp; bt < nbatches; bt += nwarps) {
     const uint64_t r = bt * kRowsPerWarp + grp;
@@ -54,7 +56,7 @@ k_spmv(CsrView X, const float* __restrict__ v, const float* __restrict__ sd,
         for (int k = 0; k < 4; ++k) {
           const int64_t e = b + k;
           if (e >= e0 && e < e1)
-            acc += norm_count(qq[k] & 0xffffu, f) * w[qq[k] >> 16];
+            acc += norm_count(qq[k] & 0xffffu, f) * w[(qq[k] >> 16) & gm];
         }
       }
     } else {
@@ -121,7 +123,7 @@ k_rmat_partials(CscView X, const float* __restrict__ u,
         for (int k = 0; k < 4; ++k) {
           const int64_t e = b + k;
           if (e >= e0 && e < e1) {
-            const uint32_t lr = qq[k] >> 16;
+            const uint32_t lr = (qq[k] >> 16) & (P - 1);  // bit 31 may flag a segment head
             acc += norm_count(qq[k] & 0xffffu, fs[lr]) * us[lr];
           }
         }
@@ -180,7 +182,7 @@ k_gene_moments(CscView X, double2* __restrict__ partials, uint32_t colgroup) {
         const uint32_t qq[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const uint32_t lr = qq[k] >> 16;
+          const uint32_t lr = (qq[k] >> 16) & (P - 1);  // bit 31 may flag a segment head
           const int64_t e = b + k;
           vals[k] = (e >= e0 && e < e1)
                         ? (X.post ? norm_count(qq[k] & 0xffffu, fs[lr]) * qs[lr]

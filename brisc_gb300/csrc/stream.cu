@@ -60,7 +60,8 @@ __device__ __forceinline__ uint4 clip_window(uint4 q, int lo, int hi) {
 __device__ __noinline__ float csr_row_exact8(const uint32_t* __restrict__ packed,
                                              int64_t e0, int64_t e1,
                                              const float* __restrict__ tb, float isf,
-                                             const float* __restrict__ w, int lane8) {
+                                             const float* __restrict__ w, uint32_t gm,
+                                             int lane8) {
   float acc = 0.f;
   for (int64_t b = (e0 & ~3ll) + 4 * lane8; b - 4 * lane8 < e1; b += 32) {
     const uint4 r4 = b < e1 ? ld_stream_u4(packed + b) : make_uint4(0, 0, 0, 0);
@@ -70,29 +71,7 @@ __device__ __noinline__ float csr_row_exact8(const uint32_t* __restrict__ packed
     for (int j = 0; j < 4; ++j) {
       const uint32_t cnt = qq[j] & 0xffffu;
       const float val = cnt < (uint32_t)kCountTab ? tb[cnt] : norm_count(cnt, isf);
-      if (vm & (1u << j)) acc += val * w[qq[j] >> 16];
-    }
-  }
-  return acc;
-}
-
-__device__ __noinline__ float csc_seg_exact8(const uint32_t* __restrict__ packed,
-                                             int64_t e0, int64_t e1,
-                                             const float* __restrict__ tab,
-                                             const float* __restrict__ us,
-                                             const float* __restrict__ isf_rows,
-                                             uint32_t pshift, int lane8) {
-  float acc = 0.f;
-  for (int64_t b = (e0 & ~3ll) + 4 * lane8; b - 4 * lane8 < e1; b += 32) {
-    const uint4 r4 = b < e1 ? ld_stream_u4(packed + b) : make_uint4(0, 0, 0, 0);
-    const uint32_t vm = window_mask(b, e0, e1);
-    const uint32_t qq[4] = {r4.x, r4.y, r4.z, r4.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t lr = qq[j] >> 16, cnt = qq[j] & 0xffffu;
-      const float val = cnt < (uint32_t)kCountTab ? tab[(cnt << pshift) + lr]
-                                                  : norm_count(cnt, isf_rows[lr]);
-      if (vm & (1u << j)) acc += val * us[lr];
+      if (vm & (1u << j)) acc += val * w[(qq[j] >> 16) & gm];
     }
   }
   return acc;
@@ -102,7 +81,7 @@ __device__ __noinline__ float csc_seg_exact8(const uint32_t* __restrict__ packed
 // X.v, counts layout: 8 lanes per cell row.
 constexpr int kTabSlot = 17;  // padded per-group table slot (conflict-free)
 
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256, 4)
 k_spmv_rows(CsrView X, const float* __restrict__ v, const float* __restrict__ sd,
             float* __restrict__ y) {
   extern __shared__ __align__(16) float sm[];
@@ -115,75 +94,126 @@ k_spmv_rows(CsrView X, const float* __restrict__ v, const float* __restrict__ sd
   const int lane8 = threadIdx.x & 7;
   const unsigned gmask = 0xFFu << (threadIdx.x & 24);
   const uint32_t gslot = (threadIdx.x >> 3) * 2 * kTabSlot;
+  // bit 31 of a stored word flags a row head when genes fit in 15 bits
+  const uint32_t gm = X.g > 32768u ? 0xffffu : 0x7fffu;
   const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 3;
   const uint64_t ngroups = (gridDim.x * (uint64_t)blockDim.x) >> 3;
   const float2* rt2 = reinterpret_cast<const float2*>(X.rtab);
 
-  int64_t nx0 = 0, nx1 = 0;  // prefetched offsets of the next row
-  if (gid < X.n) { nx0 = X.rowptr[gid]; nx1 = X.rowptr[gid + 1]; }
+  // offsets and count table of the next row, loaded one row ahead
+  int64_t nx0 = 0, nx1 = 0;
+  float2 nt2 = make_float2(0.f, 0.f);
+  if (gid < X.n) {
+    nx0 = X.rowptr[gid];
+    nx1 = X.rowptr[gid + 1];
+    nt2 = rt2[gid * (kCountTab / 2) + lane8];
+  }
   int buf = 0;
   for (uint64_t r = gid; r < X.n; r += ngroups, buf ^= 1) {
     const int64_t e0 = nx0, e1 = nx1;
-    const uint64_t rn = r + ngroups;
-    if (rn < X.n) { nx0 = X.rowptr[rn]; nx1 = X.rowptr[rn + 1]; }
-    // the row's count table into this group's (double-buffered) slot
-    float* tb = tabs + gslot + buf * kTabSlot;
-    const float2 t2 = rt2[r * (kCountTab / 2) + lane8];
-    tb[2 * lane8] = t2.x;
-    tb[2 * lane8 + 1] = t2.y;
-    __syncwarp(gmask);
+    const float2 t2 = nt2;
     // row-relative 32-bit offsets: the row's words are [lead, len) of the
     // 16-byte-aligned span starting at a0
     const int64_t a0 = e0 & ~3ll;
     const uint32_t* rowp = X.packed + a0;
     const int lead = (int)(e0 - a0), len = (int)(e1 - a0);
+    // the row's first 128 words: four 16-byte loads per lane in flight
+    const int o = 4 * lane8;
+    const uint4 z4 = make_uint4(0, 0, 0, 0);
+    const uint4 q0 = o < len ? ld_stream_u4(rowp + o) : z4;
+    const uint4 q1 = o + 32 < len ? ld_stream_u4(rowp + o + 32) : z4;
+    const uint4 q2 = o + 64 < len ? ld_stream_u4(rowp + o + 64) : z4;
+    const uint4 q3 = o + 96 < len ? ld_stream_u4(rowp + o + 96) : z4;
+    const uint64_t rn = r + ngroups;
+    if (rn < X.n) {
+      nx0 = X.rowptr[rn];
+      nx1 = X.rowptr[rn + 1];
+      nt2 = rt2[rn * (kCountTab / 2) + lane8];
+    }
+    // the row's count table into this group's (double-buffered) slot
+    float* tb = tabs + gslot + buf * kTabSlot;
+    tb[2 * lane8] = t2.x;
+    tb[2 * lane8 + 1] = t2.y;
+    __syncwarp(gmask);
     float acc = 0.f;
     uint32_t big = 0;  // OR of the loaded words: a count >= 16 shows in 0xfff0
     auto consume = [&](uint4 q, int at) {
       if (at < lead || at + 4 > len) q = clip_window(q, lead - at, len - at);
       big |= q.x | q.y | q.z | q.w;
-      acc = fmaf(tb[q.x & (kCountTab - 1)], w[q.x >> 16], acc);
-      acc = fmaf(tb[q.y & (kCountTab - 1)], w[q.y >> 16], acc);
-      acc = fmaf(tb[q.z & (kCountTab - 1)], w[q.z >> 16], acc);
-      acc = fmaf(tb[q.w & (kCountTab - 1)], w[q.w >> 16], acc);
+      acc = fmaf(tb[q.x & (kCountTab - 1)], w[(q.x >> 16) & gm], acc);
+      acc = fmaf(tb[q.y & (kCountTab - 1)], w[(q.y >> 16) & gm], acc);
+      acc = fmaf(tb[q.z & (kCountTab - 1)], w[(q.z >> 16) & gm], acc);
+      acc = fmaf(tb[q.w & (kCountTab - 1)], w[(q.w >> 16) & gm], acc);
     };
-    for (int o = 4 * lane8; o - 4 * lane8 < len; o += 64) {
-      const uint4 q0 = o < len ? ld_stream_u4(rowp + o) : make_uint4(0, 0, 0, 0);
-      const uint4 q1 = o + 32 < len ? ld_stream_u4(rowp + o + 32) : make_uint4(0, 0, 0, 0);
-      if (o < len) consume(q0, o);
-      if (o + 32 < len) consume(q1, o + 32);
+    if (o < len) consume(q0, o);
+    if (o + 32 < len) consume(q1, o + 32);
+    if (o + 64 < len) consume(q2, o + 64);
+    if (o + 96 < len) consume(q3, o + 96);
+    for (int ob = 128; ob < len; ob += 64) {  // rows longer than 128 words
+      const int oo = ob + o;
+      const uint4 p0 = oo < len ? ld_stream_u4(rowp + oo) : z4;
+      const uint4 p1 = oo + 32 < len ? ld_stream_u4(rowp + oo + 32) : z4;
+      if (oo < len) consume(p0, oo);
+      if (oo + 32 < len) consume(p1, oo + 32);
     }
     if (__any_sync(gmask, (big & 0xfff0u) != 0u))
-      acc = csr_row_exact8(X.packed, e0, e1, tb, X.isf[r], w, lane8);
+      acc = csr_row_exact8(X.packed, e0, e1, tb, X.isf[r], w, gm, lane8);
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
+    for (int s2 = 4; s2 > 0; s2 >>= 1) acc += __shfl_xor_sync(gmask, acc, s2);
     if (lane8 == 0) y[r] = X.post ? acc * X.post[r] : acc;
   }
 }
 
 // ---------------------------------------------------------------------------
-// X^T.u, counts layout: 8 lanes per (panel, gene) segment.
-struct PanelLayout {
-  uint32_t tab, us, cps, total;
-  __host__ __device__ PanelLayout(uint32_t P, uint32_t g) {
-    tab = 128;
-    us = tab + r128(P * kCountTab * 4);
-    cps = us + r128(P * 4);
-    total = cps + r128((g + 1) * 4);
+// X^T.u, counts layout: one CTA per row panel, the panel's words as one flat
+// stream. The first word of every (panel, gene) segment carries a head flag
+// (bit 31); warps take contiguous runs of whole segments, lanes take 8
+// consecutive words, and a warp-segmented scan closes each segment where the
+// next head starts. No lane idles on short segments.
+constexpr uint32_t kHeadBit = 0x80000000u;
+constexpr int kSegThreads = 512;
+constexpr int kMaxPanelRows = 2048;  // rows per panel the staged table allows
+constexpr int kSegWarps = kSegThreads / 32;
+
+struct SegLayout {
+  uint32_t tab, cps, nz, misc, total;
+  __host__ __device__ SegLayout(uint32_t P, uint32_t g) {
+    tab = 128;                             // mbarrier
+    cps = tab + r128(P * kCountTab * 4);   // table scaled by u: [count][row]
+    nz = cps + r128((g + 1) * 4);          // gene offsets, then per-gene sums
+    misc = nz + r128(g * 2);               // non-empty genes in order (u16)
+    total = misc + 128;                    // warp totals
   }
 };
 
-__global__ void __launch_bounds__(512, 2)
-k_rmat_panels(CscView X, const float* __restrict__ u, const float* __restrict__ u_scale,
-              float* __restrict__ u_out, float* __restrict__ partT,
-              int* __restrict__ err) {
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// u * scale (* post) of panel row r, as the product kernels stage it.
+__device__ __forceinline__ float scaled_u(const CscView& X, const float* u,
+                                          const float* u_scale, float scale,
+                                          uint64_t r) {
+  const float uu = u_scale ? u[r] * scale : u[r];
+  return X.post ? uu * X.post[r] : uu;
+}
+
+__global__ void __launch_bounds__(kSegThreads, 2)
+k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_scale,
+           float* __restrict__ u_out, float* __restrict__ partT,
+           int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t P = 1u << X.pshift;
-  const PanelLayout L(P, X.g);
+  const SegLayout L(P, X.g);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-  const float* tab = reinterpret_cast<const float*>(smem + L.tab);  // [c][row]
-  float* us = reinterpret_cast<float*>(smem + L.us);
+  float* ut = reinterpret_cast<float*>(smem + L.tab);      // [count][row]
   int32_t* cps = reinterpret_cast<int32_t*>(smem + L.cps);
+  float* gsum = reinterpret_cast<float*>(smem + L.cps);    // after the ranges
+  uint16_t* nz = reinterpret_cast<uint16_t*>(smem + L.nz);
+  int32_t* wtot = reinterpret_cast<int32_t*>(smem + L.misc);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
   const uint32_t p = blockIdx.x;
   const uint64_t r0 = (uint64_t)p << X.pshift;
@@ -196,50 +226,359 @@ k_rmat_panels(CscView X, const float* __restrict__ u, const float* __restrict__ 
     bulk_g2s(smem + L.tab, X.rtab + (uint64_t)p * kCountTab * P, tb, &bar[0]);
   }
   const float scale = u_scale ? *u_scale : 1.f;
-  for (uint32_t i = threadIdx.x; i < rows; i += blockDim.x) {
-    const float uu = u_scale ? u[r0 + i] * scale : u[r0 + i];
-    if (u_out) u_out[r0 + i] = uu;
-    us[i] = X.post ? uu * X.post[r0 + i] : uu;
+  float usr[kMaxPanelRows / kSegThreads];
+#pragma unroll
+  for (int k = 0; k < kMaxPanelRows / kSegThreads; ++k) {
+    const uint32_t i = threadIdx.x + k * kSegThreads;
+    float us = 0.f;
+    if (i < rows) {
+      if (u_out) u_out[r0 + i] = u_scale ? u[r0 + i] * scale : u[r0 + i];
+      us = scaled_u(X, u, u_scale, scale, r0 + i);
+    }
+    usr[k] = us;
   }
-  for (uint32_t i = rows + threadIdx.x; i < P; i += blockDim.x) us[i] = 0.f;
   const int32_t* cp = X.colptr + (uint64_t)p * (X.g + 1);
-  for (uint32_t c = threadIdx.x; c <= X.g; c += blockDim.x) cps[c] = cp[c];
-  __syncthreads();  // barrier initialised, us/cps staged
+  for (uint32_t c = threadIdx.x; c <= X.g; c += kSegThreads) cps[c] = cp[c];
+  __syncthreads();
+
+  // Non-empty genes of the panel, in gene order.
+  uint32_t S = 0;
+  for (uint32_t base = 0; base < X.g; base += kSegThreads) {
+    const uint32_t c = base + threadIdx.x;
+    const bool f = c < X.g && cps[c + 1] > cps[c];
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wtot[wid] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+#pragma unroll
+    for (int j = 0; j < kSegWarps; ++j) {
+      const uint32_t t = (uint32_t)wtot[j];
+      before += j < wid ? t : 0u;
+      tot += t;
+    }
+    if (f) nz[S + before + __popc(bal & lanemask_lt())] = (uint16_t)c;
+    S += tot;
+    __syncthreads();
+  }
+  const uint32_t W = (uint32_t)cps[X.g];
+
+  // The table arrives; scale it by u in place (count 0 stays 0).
+  const bool ok = __syncthreads_and(mbar_wait(&bar[0], 0, err));
+  if (!ok) return;  // every thread waited (bounded) for the copy
+#pragma unroll
+  for (int k = 0; k < kMaxPanelRows / kSegThreads; ++k) {
+    const uint32_t i = threadIdx.x + k * kSegThreads;
+    if (i < P)
+#pragma unroll
+      for (int c = 1; c < kCountTab; ++c) ut[c * P + i] *= usr[k];
+  }
+
+  // This warp's run of segments: ordinals [i0, i1), words [s0, s1).
+  auto first_at = [&](uint64_t t) {  // first ordinal whose segment starts >= t
+    uint32_t lo = 0, hi = S;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if ((uint64_t)cps[nz[mid]] < t) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  };
+  const uint32_t i0 = first_at((uint64_t)W * wid / kSegWarps);
+  const uint32_t i1 = wid == kSegWarps - 1 ? S : first_at((uint64_t)W * (wid + 1) / kSegWarps);
+  const uint32_t s0 = i0 < S ? (uint32_t)cps[nz[i0]] : W;
+  const uint32_t s1 = i1 < S ? (uint32_t)cps[nz[i1]] : W;
+  __syncthreads();  // cps is no longer read: its space holds the gene sums
+  for (uint32_t c = threadIdx.x; c < X.g; c += kSegThreads) gsum[c] = 0.f;
+  __syncthreads();
+
+  const int64_t pbase = X.rowptr[r0];
+  const int64_t beg = pbase + s0, end = pbase + s1;
+  const uint32_t pshift = X.pshift, lrmask = P - 1;
+  const uint32_t lt = lanemask_lt();
+  float carry = 0.f;  // open segment's sum entering the next iteration
+  uint32_t kb = 0;    // heads seen in earlier iterations
+  for (int64_t b = beg & ~7ll; b < end; b += 256) {
+    const int64_t wb = b + 8 * lane;
+    uint4 qa = make_uint4(0, 0, 0, 0), qb = qa;
+    if (wb < end) {
+      qa = ld_stream_u4(X.packed + wb);
+      qb = ld_stream_u4(X.packed + wb + 4);
+    }
+    uint32_t wd[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+    if (wb < beg || wb + 8 > end) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (wb + i < beg || wb + i >= end) wd[i] = 0u;
+    }
+    float v[8];
+    uint32_t big = 0, hm = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      big |= wd[i];
+      hm |= (wd[i] >> 31) << i;
+      v[i] = ut[((wd[i] & (kCountTab - 1)) << pshift) | ((wd[i] >> 16) & lrmask)];
+    }
+    if (__any_sync(0xffffffffu, (big & 0xfff0u) != 0u)) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t cnt = wd[i] & 0xffffu;
+        if (cnt >= (uint32_t)kCountTab) {
+          const uint64_t r = r0 + ((wd[i] >> 16) & lrmask);
+          v[i] = norm_count(cnt, X.isf[r]) * scaled_u(X, u, u_scale, scale, r);
+        }
+      }
+    }
+    // in-lane segmented sums: s[i] = sum since the last head at or before i
+    float sl[8];
+    sl[0] = v[0];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) sl[i] = ((hm >> i) & 1u) ? v[i] : sl[i - 1] + v[i];
+    const uint32_t F = __ballot_sync(0xffffffffu, hm != 0u);
+    // cross-lane inclusive segmented scan of the lane tails
+    float T = sl[7];
+    uint32_t fa = hm != 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const float Tp = __shfl_up_sync(0xffffffffu, T, d);
+      const uint32_t fp = __shfl_up_sync(0xffffffffu, fa, d);
+      if (lane >= d) {
+        if (!fa) T = Tp + T;
+        fa |= fp;
+      }
+    }
+    if ((F & (lt | (1u << lane))) == 0u) T = carry + T;  // no head up to here
+    float cin = __shfl_up_sync(0xffffffffu, T, 1);
+    if (lane == 0) cin = carry;  // open sum entering this lane
+    // heads in earlier lanes of this iteration
+    const uint32_t h = __popc(hm);
+    uint32_t hs = h;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, hs, d);
+      if (lane >= d) hs += t;
+    }
+    const uint32_t kl = kb + hs - h;  // heads before this lane
+    // a head closes the segment before it (the run's first head closes nothing)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((hm >> i) & 1u) {
+        const uint32_t pre = hm & ((1u << i) - 1u);
+        const uint32_t k = kl + __popc(pre);
+        if (k > 0) {
+          const float val = i == 0 ? cin : (pre ? sl[i - 1] : cin + sl[i - 1]);
+          gsum[nz[i0 + k - 1]] = val;
+        }
+      }
+    }
+    carry = __shfl_sync(0xffffffffu, T, 31);
+    kb += __shfl_sync(0xffffffffu, hs, 31);
+  }
+  if (lane == 0 && kb > 0) gsum[nz[i0 + kb - 1]] = carry;
+  __syncthreads();
+  for (uint32_t c = threadIdx.x; c < X.g; c += kSegThreads)
+    partT[(uint64_t)c * X.num_panels + p] = gsum[c];
+}
+
+// ---------------------------------------------------------------------------
+// X.v, counts layout with row heads (genes < 32768): one CTA per row panel,
+// the panel's CSR words as one flat stream, the same warp-segmented scan as
+// X^T.u with rows as the segments. The panel's count table ([count][row],
+// shared with X^T.u) arrives by bulk copy; each lane tracks the row of its
+// words from the head flags.
+struct RowSegLayout {
+  uint32_t tab, w, rofs, nzr, rsum, misc, total;
+  __host__ __device__ RowSegLayout(uint32_t P, uint32_t g) {
+    tab = 128;                             // mbarrier
+    w = tab + r128(P * kCountTab * 4);     // count table [count][row]
+    rofs = w + r128(g * 4);                // v / sd
+    nzr = rofs + r128((P + 1) * 4);        // row offsets in the panel
+    rsum = nzr + r128(P * 2);              // non-empty rows in order (u16)
+    misc = rsum + r128(P * 4);             // per-row sums
+    total = misc + 128;                    // warp totals
+  }
+};
+
+__global__ void __launch_bounds__(kSegThreads, 2)
+k_spmv_seg(CsrView X, uint32_t pshift, const float* __restrict__ rtab_c,
+           const float* __restrict__ v, const float* __restrict__ sd,
+           float* __restrict__ y, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t P = 1u << pshift;
+  const RowSegLayout L(P, X.g);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  const float* tab = reinterpret_cast<const float*>(smem + L.tab);
+  float* wv = reinterpret_cast<float*>(smem + L.w);
+  int32_t* rofs = reinterpret_cast<int32_t*>(smem + L.rofs);
+  uint16_t* nzr = reinterpret_cast<uint16_t*>(smem + L.nzr);
+  float* rsum = reinterpret_cast<float*>(smem + L.rsum);
+  int32_t* wtot = reinterpret_cast<int32_t*>(smem + L.misc);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+
+  const uint32_t p = blockIdx.x;
+  const uint64_t r0 = (uint64_t)p << pshift;
+  const uint32_t rows = (uint32_t)min_u64(P, X.n - r0);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    fence_mbar_init();
+    const uint32_t tb = P * kCountTab * 4;
+    mbar_arrive_expect_tx(&bar[0], tb);
+    bulk_g2s(smem + L.tab, rtab_c + (uint64_t)p * kCountTab * P, tb, &bar[0]);
+  }
+  for (uint32_t c = threadIdx.x; c < X.g; c += kSegThreads)
+    wv[c] = sd ? v[c] / sd[c] : v[c];  // pca.pyx:461-462
+  const int64_t pbase = X.rowptr[r0];
+  for (uint32_t i = threadIdx.x; i <= P; i += kSegThreads)
+    rofs[i] = (int32_t)(X.rowptr[r0 + min(i, rows)] - pbase);
+  for (uint32_t i = threadIdx.x; i < P; i += kSegThreads) rsum[i] = 0.f;
+  __syncthreads();
+
+  // Non-empty rows of the panel, in order.
+  uint32_t S = 0;
+  for (uint32_t base = 0; base < rows; base += kSegThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const bool f = i < rows && rofs[i + 1] > rofs[i];
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wtot[wid] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+#pragma unroll
+    for (int j = 0; j < kSegWarps; ++j) {
+      const uint32_t t = (uint32_t)wtot[j];
+      before += j < wid ? t : 0u;
+      tot += t;
+    }
+    if (f) nzr[S + before + __popc(bal & lanemask_lt())] = (uint16_t)i;
+    S += tot;
+    __syncthreads();
+  }
+  const uint32_t W = (uint32_t)rofs[rows];
+  auto first_at = [&](uint64_t t) {  // first ordinal whose row starts >= t
+    uint32_t lo = 0, hi = S;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if ((uint64_t)rofs[nzr[mid]] < t) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  };
+  const uint32_t i0 = first_at((uint64_t)W * wid / kSegWarps);
+  const uint32_t i1 = wid == kSegWarps - 1 ? S : first_at((uint64_t)W * (wid + 1) / kSegWarps);
+  const uint32_t s0 = i0 < S ? (uint32_t)rofs[nzr[i0]] : W;
+  const uint32_t s1 = i1 < S ? (uint32_t)rofs[nzr[i1]] : W;
   const bool ok = __syncthreads_and(mbar_wait(&bar[0], 0, err));
   if (!ok) return;  // every thread waited (bounded) for the copy
 
-  const int64_t pbase = X.rowptr[r0];
-  const int lane8 = threadIdx.x & 7;
-  const unsigned gmask = 0xFFu << (threadIdx.x & 24);
-  const uint32_t pshift = X.pshift;
-  for (uint32_t c = threadIdx.x >> 3; c < X.g; c += blockDim.x >> 3) {
-    const int64_t e0 = pbase + cps[c], e1 = pbase + cps[c + 1];
-    const int64_t a0 = e0 & ~3ll;
-    const uint32_t* segp = X.packed + a0;
-    const int lead = (int)(e0 - a0), len = (int)(e1 - a0);
-    float acc = 0.f;
-    uint32_t big = 0;
-    auto consume = [&](uint4 q, int at) {
-      if (at < lead || at + 4 > len) q = clip_window(q, lead - at, len - at);
-      big |= q.x | q.y | q.z | q.w;
-      // a zeroed word reads tab[0][row 0] = 0
-      acc = fmaf(tab[((q.x & (kCountTab - 1)) << pshift) + (q.x >> 16)], us[q.x >> 16], acc);
-      acc = fmaf(tab[((q.y & (kCountTab - 1)) << pshift) + (q.y >> 16)], us[q.y >> 16], acc);
-      acc = fmaf(tab[((q.z & (kCountTab - 1)) << pshift) + (q.z >> 16)], us[q.z >> 16], acc);
-      acc = fmaf(tab[((q.w & (kCountTab - 1)) << pshift) + (q.w >> 16)], us[q.w >> 16], acc);
-    };
-    for (int o = 4 * lane8; o - 4 * lane8 < len; o += 64) {
-      const uint4 q0 = o < len ? ld_stream_u4(segp + o) : make_uint4(0, 0, 0, 0);
-      const uint4 q1 = o + 32 < len ? ld_stream_u4(segp + o + 32) : make_uint4(0, 0, 0, 0);
-      if (o < len) consume(q0, o);
-      if (o + 32 < len) consume(q1, o + 32);
+  const int64_t beg = pbase + s0, end = pbase + s1;
+  const uint32_t lt = lanemask_lt();
+  float carry = 0.f;
+  uint32_t kb = 0;
+  for (int64_t b = beg & ~7ll; b < end; b += 256) {
+    const int64_t wb = b + 8 * lane;
+    uint4 qa = make_uint4(0, 0, 0, 0), qb = qa;
+    if (wb < end) {
+      qa = ld_stream_u4(X.packed + wb);
+      qb = ld_stream_u4(X.packed + wb + 4);
     }
-    if (__any_sync(gmask, (big & 0xfff0u) != 0u))
-      acc = csc_seg_exact8(X.packed, e0, e1, tab, us, X.isf + r0, pshift, lane8);
+    uint32_t wd[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+    if (wb < beg || wb + 8 > end) {
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o);
-    if (lane8 == 0) partT[(uint64_t)c * X.num_panels + p] = acc;
+      for (int i = 0; i < 8; ++i)
+        if (wb + i < beg || wb + i >= end) wd[i] = 0u;
+    }
+    uint32_t hm = 0, big = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      hm |= (wd[i] >> 31) << i;
+      big |= wd[i];
+    }
+    // heads in earlier lanes of this iteration
+    const uint32_t h = __popc(hm);
+    uint32_t hs = h;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, hs, d);
+      if (lane >= d) hs += t;
+    }
+    const uint32_t kl = kb + hs - h;  // heads before this lane
+    // row of the open segment entering the lane (row 0 reads table slot 0
+    // of a zeroed word before the run's first head)
+    const uint32_t rin = kl > 0 ? nzr[i0 + kl - 1] : 0u;
+    float sl[8];
+    {
+      uint32_t cur = rin, k = kl;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if ((hm >> i) & 1u) cur = nzr[i0 + k++];
+        const float t = tab[((wd[i] & (kCountTab - 1)) << pshift) | cur];
+        sl[i] = t * wv[(wd[i] >> 16) & 0x7fffu];
+      }
+    }
+    if (__any_sync(0xffffffffu, (big & 0xfff0u) != 0u)) {
+      uint32_t cur = rin, k = kl;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if ((hm >> i) & 1u) cur = nzr[i0 + k++];
+        const uint32_t cnt = wd[i] & 0xffffu;
+        if (cnt >= (uint32_t)kCountTab)
+          sl[i] = norm_count(cnt, X.isf[r0 + cur]) * wv[(wd[i] >> 16) & 0x7fffu];
+      }
+    }
+    // in-lane segmented sums
+#pragma unroll
+    for (int i = 1; i < 8; ++i) sl[i] = ((hm >> i) & 1u) ? sl[i] : sl[i - 1] + sl[i];
+    const uint32_t F = __ballot_sync(0xffffffffu, hm != 0u);
+    float T = sl[7];
+    uint32_t fa = hm != 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const float Tp = __shfl_up_sync(0xffffffffu, T, d);
+      const uint32_t fp = __shfl_up_sync(0xffffffffu, fa, d);
+      if (lane >= d) {
+        if (!fa) T = Tp + T;
+        fa |= fp;
+      }
+    }
+    if ((F & (lt | (1u << lane))) == 0u) T = carry + T;
+    float cin = __shfl_up_sync(0xffffffffu, T, 1);
+    if (lane == 0) cin = carry;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((hm >> i) & 1u) {
+        const uint32_t pre = hm & ((1u << i) - 1u);
+        const uint32_t k = kl + __popc(pre);
+        if (k > 0) {
+          const float val = i == 0 ? cin : (pre ? sl[i - 1] : cin + sl[i - 1]);
+          rsum[nzr[i0 + k - 1]] = val;
+        }
+      }
+    }
+    carry = __shfl_sync(0xffffffffu, T, 31);
+    kb += __shfl_sync(0xffffffffu, hs, 31);
   }
+  if (lane == 0 && kb > 0) rsum[nzr[i0 + kb - 1]] = carry;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < rows; i += kSegThreads)
+    y[r0 + i] = X.post ? rsum[i] * X.post[r0 + i] : rsum[i];
+}
+
+// Row heads (matrix creation): bit 31 of the first word of every non-empty
+// CSR row (gene indices then fit in bits 16-30).
+__global__ void k_mark_row_heads(const int64_t* __restrict__ rowptr, uint64_t n,
+                                 uint32_t* __restrict__ packed) {
+  const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r < n && rowptr[r + 1] > rowptr[r]) packed[rowptr[r]] |= kHeadBit;
+}
+
+// Head flags (matrix creation): bit 31 of the first word of every non-empty
+// (panel, gene) segment of the transposed copy.
+__global__ void k_mark_heads(const int64_t* __restrict__ rowptr,
+                             const int32_t* __restrict__ colptr, uint64_t n,
+                             uint32_t g, uint32_t pshift, uint32_t num_panels,
+                             uint32_t* __restrict__ packed) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)num_panels * g) return;
+  const uint64_t p = i / g;
+  const uint32_t c = (uint32_t)(i % g);
+  const int32_t* cp = colptr + p * (g + 1);
+  if (cp[c + 1] > cp[c]) packed[rowptr[p << pshift] + cp[c]] |= kHeadBit;
 }
 
 // z[c] = (sum over panels in panel order of partT[c][p]) / sd[c]; one warp per
@@ -278,8 +617,8 @@ __global__ void k_count_tables(const float* __restrict__ isf, uint64_t n,
 }  // namespace
 
 bool stream_supported(const Matrix& m) {
-  return m.mode == kCounts && m.P <= 2048 &&
-         PanelLayout(m.P, m.g).total <= 113 * 1024;
+  return m.mode == kCounts && m.P <= (uint32_t)kMaxPanelRows &&
+         SegLayout(m.P, m.g).total <= 220 * 1024;
 }
 
 int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
@@ -295,19 +634,37 @@ int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
   k_count_tables<<<(unsigned)ceil_div(nr, 256), 256, 0, s>>>(
       m->isf, m->n, m->pshift, m->rtab_r, m->rtab_c);
   BGPU_CHECK_LAUNCH();
+  const uint64_t segs = (uint64_t)m->num_panels * m->g;
+  k_mark_heads<<<(unsigned)ceil_div(segs, 256), 256, 0, s>>>(
+      m->rowptr, m->colptr, m->n, m->g, m->pshift, m->num_panels, m->csc_packed);
+  BGPU_CHECK_LAUNCH();
+  m->csr_heads = m->g <= 32768u && RowSegLayout(m->P, m->g).total <= 220 * 1024;
+  if (m->csr_heads) {
+    k_mark_row_heads<<<(unsigned)ceil_div(m->n, 256), 256, 0, s>>>(m->rowptr, m->n,
+                                                                    m->csr_packed);
+    BGPU_CHECK_LAUNCH();
+  }
   m->stream_ok = true;
   return BGPU_OK;
 }
 
 int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
                          float* y, int* err, cudaStream_t s) {
-  (void)err;
   const CsrView X = csr_view(m);
+  if (m.csr_heads && m.spmv_seg) {
+    const size_t smem = RowSegLayout(m.P, m.g).total;
+    BGPU_CUDA(cudaFuncSetAttribute(k_spmv_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    k_spmv_seg<<<m.num_panels, kSegThreads, smem, s>>>(X, m.pshift, m.rtab_c, v, sd,
+                                                       y, err);
+    BGPU_CHECK_LAUNCH();
+    return BGPU_OK;
+  }
   const size_t smem = ((size_t)((m.g + 3) & ~3u) + 32 * 2 * kTabSlot) * 4;
   if (smem > 48 * 1024)
     BGPU_CUDA(cudaFuncSetAttribute(k_spmv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-  k_spmv_rows<<<num_sms() * 5, 256, smem, s>>>(X, v, sd, y);
+  k_spmv_rows<<<num_sms() * 4, 256, smem, s>>>(X, v, sd, y);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -315,10 +672,10 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
 int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
                           float* u_out, float* partT, int* err, cudaStream_t s) {
   const CscView X = csc_view(m);
-  const size_t smem = PanelLayout(m.P, m.g).total;
-  BGPU_CUDA(cudaFuncSetAttribute(k_rmat_panels, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const size_t smem = SegLayout(m.P, m.g).total;
+  BGPU_CUDA(cudaFuncSetAttribute(k_rmat_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-  k_rmat_panels<<<m.num_panels, 512, smem, s>>>(X, u, u_scale, u_out, partT, err);
+  k_rmat_seg<<<m.num_panels, kSegThreads, smem, s>>>(X, u, u_scale, u_out, partT, err);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

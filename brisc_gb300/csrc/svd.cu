@@ -6,8 +6,8 @@
 // rotated pairwise until mutually orthogonal; the accumulated rotations J
 // give Ub = J, the column norms give Sb and the normalised columns give the
 // rows of Vbt. Pairs are visited in a fixed round-robin (circle) schedule,
-// m/2 disjoint pairs per round, one warp per pair, so the result does not
-// depend on timing. Arithmetic is FP32: GB300's FP64 rate is a small fraction
+// m/2 disjoint pairs per round, one 8-lane group per pair, so the result
+// does not depend on timing. Arithmetic is FP32: GB300's FP64 rate is a small fraction
 // of its FP32 rate, and an O(m^3) FP64 Jacobi on one SM would cost more than
 // the Lanczos steps it serves; the reference itself uses FP32 (sgesdd).
 #include <algorithm>
@@ -67,46 +67,54 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
     J[t] = (t / m == t % m) ? T(1) : T(0);
   __syncthreads();
 
+  // Pairs go to 8-lane groups (up to 128 disjoint pairs per round at once):
+  // 8-lane reductions are 3 shuffle levels instead of 5.
   const int M2 = (int)m + ((int)m & 1);
+  const int l8 = threadIdx.x & 7;
+  const unsigned gm8 = 0xFFu << (lane & 24);
+  const int grp = threadIdx.x >> 3, ngrp = blockDim.x >> 3;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) rotated = 0;
     __syncthreads();
     for (int round = 0; round < M2 - 1; ++round) {
-      for (int idx = wid; idx < M2 / 2; idx += nw) {
+      for (int idx = grp; idx < M2 / 2; idx += ngrp) {
         int p, q;
         pair_of(round, idx, M2, &p, &q);
         if (q >= (int)m) continue;
         T* ap = A + (uint64_t)p * la;
         T* aq = A + (uint64_t)q * la;
         T al = 0, be = 0, ga = 0;
-        for (int r = lane; r < la; r += 32) {
+        for (int r = l8; r < la; r += 8) {
           const T x = ap[r], y = aq[r];
           al += x * x;
           be += y * y;
           ga += x * y;
         }
-        al = warp_sum_t(al);
-        be = warp_sum_t(be);
-        ga = warp_sum_t(ga);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+          al += __shfl_xor_sync(gm8, al, o);
+          be += __shfl_xor_sync(gm8, be, o);
+          ga += __shfl_xor_sync(gm8, ga, o);
+        }
         if (al > T(0) && be > T(0) && fabs(ga) > thresh * sqrt(al * be)) {
           const T zeta = (be - al) / (T(2) * ga);
           const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
           const T c = T(1) / sqrt(T(1) + t * t);
           const T sn = c * t;
-          for (int r = lane; r < la; r += 32) {
+          for (int r = l8; r < la; r += 8) {
             const T x = ap[r], y = aq[r];
             ap[r] = c * x - sn * y;
             aq[r] = sn * x + c * y;
           }
           T* jp = J + (uint64_t)p * m;
           T* jq = J + (uint64_t)q * m;
-          for (int r = lane; r < (int)m; r += 32) {
+          for (int r = l8; r < (int)m; r += 8) {
             const T x = jp[r], y = jq[r];
             jp[r] = c * x - sn * y;
             jq[r] = sn * x + c * y;
           }
-          if (lane == 0) rotated = 1;
+          if (l8 == 0) rotated = 1;
         }
       }
       __syncthreads();

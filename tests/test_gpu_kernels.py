@@ -110,10 +110,10 @@ def _normalized(X, isf, post=None):
 @pytest.mark.parametrize("mode", ["counts", "counts_post", "float"])
 @pytest.mark.parametrize("itype", [np.int32, np.int64])
 @pytest.mark.parametrize("panel_rows", [0, 2048])
-@pytest.mark.parametrize("impl", ["stream", "vector"])
+@pytest.mark.parametrize("impl", ["rows", "seg", "vector"])
 def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows, impl, monkeypatch):
     import torch
-    monkeypatch.setenv("BGPU_SPMV_LEGACY", "1" if impl == "vector" else "0")
+    monkeypatch.setenv("BGPU_SPMV_IMPL", impl)
     X, isf = _mat()
     n, g = X.shape
     post = None
