@@ -98,6 +98,7 @@ SIGNATURES = {
                             _u32, _f, _u32, _u64, _i, _i, _u32, _u64, _vp,
                             C.POINTER(_i)]),
     "bgpu_start_vector": (_i, [_u64, _u32, _vp]),
+    "bgpu_rotate_basis": (_i, [_vp, _u64, _u64, _u32, _vp, _u64, _u32, _vp, _u64, _i, _vp]),
     "bgpu_small_svd": (_i, [_vp, _u32, _vp, _vp, _vp, _vp]),
     "bgpu_small_svd_noalloc": (_i, [_vp, _u32, _vp, _vp, _vp, _vp]),
     "bgpu_size_factors": (_i, [_vp, _i, _vp, _i, _u64, _i, _vp, _vp, _vp, _vp, _vp]),

@@ -141,6 +141,7 @@ struct Solver {
       Vbt, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last, sb64, ratios,
       derr;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
+  int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
   PinnedStatus hst;
 
@@ -334,6 +335,11 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
   S.profile = o.profile != 0;
   {
     S.svd64 = o.svd_fp64 != 0;
+    BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
+    const bool tc_ok = gemm_tc_supported(o.subspace_size, o.subspace_size);
+    BGPU_REQUIRE(o.rotation_mode != 2 || tc_ok, BGPU_ERR_UNSUPPORTED,
+                 "tensor-core rotation needs subspace_size <= 112");
+    S.rot_mode = o.rotation_mode == 0 ? (tc_ok ? 2 : 1) : (int)o.rotation_mode;
     const char* et = std::getenv("BGPU_TRACE");
     S.trace = et && et[0] == '1';
   }
@@ -420,8 +426,12 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     kc = (uint32_t)last.k_current;
     // Restart rotation (pca.pyx:1210-1226): U <- U Ub[:, :kc], V <- V Vbt^T.
     BGPU_TRY(S.ev_begin(5));
-    BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1,
-                            m, nullptr, kc, S.Unew.as<float>(), S.ldu, false, s));
+    if (S.rot_mode == 2)
+      BGPU_TRY(launch_gemm_tc(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), m, kc,
+                              S.Unew.as<float>(), S.ldu, S.derr.as<int>(), s));
+    else
+      BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1,
+                              m, nullptr, kc, S.Unew.as<float>(), S.ldu, false, s));
     BGPU_TRY(launch_gemm_ts(S.V.as<float>(), S.ldv, g, m, S.Vbt.as<float>(), m,
                             1, nullptr, kc, S.Vnew.as<float>(), S.ldv, false, s));
     BGPU_CUDA(cudaMemcpyAsync(S.Vnew.as<float>() + (uint64_t)kc * S.ldv,
@@ -612,6 +622,31 @@ extern "C" int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
   BGPU_REQUIRE(mat && opts, BGPU_ERR_INVALID, "NULL argument");
   return irlba_solve(mat->m, *opts, pcs, pcs_on_device, singular_values,
                      loadings, info, (cudaStream_t)stream);
+}
+
+extern "C" int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
+                                 uint32_t K, const float* Bm, uint64_t ldb,
+                                 uint32_t ncols, float* C, uint64_t ldc, int mode,
+                                 void* stream) {
+  BGPU_REQUIRE(A && Bm && C && K >= 1 && ncols >= 1 && ncols <= K && lda >= rows &&
+                   ldb >= K && ldc >= rows,
+               BGPU_ERR_INVALID, "bad rotation arguments");
+  BGPU_REQUIRE(mode == 1 || mode == 2, BGPU_ERR_INVALID, "mode must be 1 or 2");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (mode == 1)
+    BGPU_TRY(launch_gemm_ts(A, lda, rows, K, Bm, 1, ldb, nullptr, ncols, C, ldc,
+                            false, s));
+  else {
+    Buf err;
+    BGPU_TRY(balloc(err, 16, true, s));
+    BGPU_TRY(launch_gemm_tc(A, lda, rows, K, Bm, ldb, ncols, C, ldc, err.as<int>(), s));
+    int h = 0;
+    BGPU_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));
+    BGPU_REQUIRE(h == 0, BGPU_ERR_DEVICE, "tensor-core rotation wait timed out");
+  }
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  return BGPU_OK;
 }
 
 extern "C" int bgpu_start_vector(uint64_t seed, uint32_t num_genes,

@@ -1,0 +1,269 @@
+// Restart rotation U <- U . Ub[:, :kc] (brisc/pca.pyx:1210-1215, the
+// reference's matmul_nn_f_out of pca.pyx:578-616) on the 5th-generation tensor
+// cores: tcgen05.mma with operands in shared memory and the accumulator in
+// tensor memory (TMEM).
+//
+// Precision: FP32 operands are split as x = hi + lo with hi = x truncated to
+// TF32 (low 13 mantissa bits cleared) and lo = x - hi (exact in FP32); the
+// product is hi.hi + hi.lo + lo.hi (three kind::tf32 MMAs accumulated in FP32
+// in TMEM). The dropped lo.lo term and the TF32 reading of lo are below 2^-20
+// relative per product, so the rotation keeps FP32-level accuracy while the
+// tensor pipe carries the arithmetic (the rotation's ~25 flop/byte would need
+// ~170 TFLOP/s of FP32 to keep up with HBM).
+//
+// Shape: persistent CTAs (one per SM, 256 threads) walk 128-row tiles of U.
+// Ub's split halves are staged once per CTA; each tile of U is loaded with
+// coalesced 32-byte row runs, split and written in the canonical no-swizzle
+// K-major layout (8-row x 16-byte core matrices, K-direction core stride
+// LBO = 128 B, 8-row stride SBO = Kp/4 * 128 B); one elected thread issues
+// 3 * Kp/8 MMAs of M=128, N=Np, K=8 and commits them to an mbarrier; all 8
+// warps then read the accumulator back (tcgen05.ld, 32 lanes x 8 columns per
+// load) and store C column-major (128-byte runs per column).
+//
+// Every mbarrier wait is bounded (about 1 s of SM clock): on timeout the
+// kernel records kDevErrTimeout, stops, frees its TMEM and returns.
+#include <algorithm>
+
+#include "dense.cuh"
+#include "tma.cuh"
+
+namespace bgpu {
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcRows = 128;  // M of one MMA / rows per tile
+
+struct TcLayout {
+  uint32_t ahi, alo, bhi, blo, total;
+  __host__ __device__ TcLayout(uint32_t Kp, uint32_t Np) {
+    ahi = 1024;  // mbarrier + TMEM address slot live below
+    alo = ahi + kTcRows * Kp * 4;
+    bhi = alo + kTcRows * Kp * 4;
+    blo = bhi + Np * Kp * 4;
+    total = blo + Np * Kp * 4;
+  }
+};
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading (K) and
+// stride (8-row) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo,
+                                              uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(uint32_t M, uint32_t N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b,
+                                         uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+      ::"r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Split 4 floats into TF32 high parts and FP32 remainders.
+__device__ __forceinline__ void split4(const float (&x)[4], uint4& hi, uint4& lo) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = __float_as_uint(x[i]) & 0xFFFFE000u;
+    l[i] = __float_as_uint(x[i] - __uint_as_float(h[i]));
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Byte offset of element (row, 4*kg) in the core-matrix layout (16 bytes
+// hold k = 4kg..4kg+3 of one row).
+__device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t kg, uint32_t kq) {
+  return ((row >> 3) * kq + kg) * 128u + (row & 7u) * 16u;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
+          const float* __restrict__ Bm, uint64_t ldb, uint32_t ncols,
+          float* __restrict__ C, uint64_t ldc, uint32_t Kp, uint32_t Np,
+          uint32_t tmem_cols, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
+  __shared__ int stop;
+  const TcLayout L(Kp, Np);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t kq = Kp / 4;  // 16-byte K groups per row
+
+  if (wid == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_u32(tslot)), "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    stop = 0;
+  }
+  // B operand (N x K, K-major): row n of it is column n of Bm.
+  for (uint32_t t = tid; t < Np * kq; t += kTcThreads) {
+    const uint32_t n = t / kq, kg = t % kq;
+    float x[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t k = kg * 4 + j;
+      x[j] = (n < ncols && k < K) ? Bm[(uint64_t)n * ldb + k] : 0.f;
+    }
+    uint4 hi, lo;
+    split4(x, hi, lo);
+    *reinterpret_cast<uint4*>(smem + L.bhi + core_off(n, kg, kq)) = hi;
+    *reinterpret_cast<uint4*>(smem + L.blo + core_off(n, kg, kq)) = lo;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = idesc_tf32(kTcRows, Np);
+  const uint32_t sbo_a = kq * 128u, sbo_b = kq * 128u;
+  const uint32_t base = smem_u32(smem);
+
+  const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
+  uint32_t phase = 0;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t row0 = tile * kTcRows;
+    // A tile: task = (row group, k group, row in group); 8 lanes read 8
+    // consecutive rows of one column (32-byte runs).
+    for (uint32_t t = tid; t < kTcRows * kq; t += kTcThreads) {
+      const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
+      const uint32_t r = rg * 8 + rr;
+      const uint64_t gr = row0 + r;
+      float x[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t k = kg * 4 + j;
+        x[j] = (gr < rows && k < K) ? A[(uint64_t)k * lda + gr] : 0.f;
+      }
+      uint4 hi, lo;
+      split4(x, hi, lo);
+      *reinterpret_cast<uint4*>(smem + L.ahi + core_off(r, kg, kq)) = hi;
+      *reinterpret_cast<uint4*>(smem + L.alo + core_off(r, kg, kq)) = lo;
+    }
+    fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      for (uint32_t ks = 0; ks < Kp / 8; ++ks) {
+        const uint32_t off = ks * 256u;  // two 16-byte K groups per K=8 step
+        const uint64_t ah = smem_desc(base + L.ahi + off, 128u, sbo_a);
+        const uint64_t al = smem_desc(base + L.alo + off, 128u, sbo_a);
+        const uint64_t bh = smem_desc(base + L.bhi + off, 128u, sbo_b);
+        const uint64_t bl = smem_desc(base + L.blo + off, 128u, sbo_b);
+        mma_tf32(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
+        mma_tf32(tmem, ah, bl, idesc, 1u);
+        mma_tf32(tmem, al, bh, idesc, 1u);
+      }
+      mma_commit(bar);
+    }
+    const bool ok = mbar_wait(bar, phase, err);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) stop = 1;
+      break;
+    }
+    phase ^= 1u;
+    tc_fence_after();
+    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (tile rows), columns of
+    // its half; lane = row.
+    const uint32_t q = wid & 3u, h = wid >> 2;
+    const uint32_t half = Np / 2;
+    const uint64_t gr = row0 + q * 32 + lane;
+    for (uint32_t c0 = h * half; c0 < (h + 1) * half; c0 += 8) {
+      float v[8];
+      tmem_ld8(tmem + ((q * 32u) << 16) + c0, v);
+      if (gr < rows) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (c0 + j < ncols) C[(uint64_t)(c0 + j) * ldc + gr] = v[j];
+      }
+    }
+    tc_fence_before();
+    __syncthreads();  // TMEM read and smem A free before the next tile
+  }
+  __syncthreads();
+  if (stop) {
+    // the timed-out commit may still be outstanding: give it one more bounded
+    // wait before the TMEM goes back
+    (void)mbar_wait(bar, phase, nullptr);
+  }
+  tc_fence_after();
+  if (wid == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 ::"r"(tmem), "r"(tmem_cols)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+bool gemm_tc_supported(uint32_t K, uint32_t ncols) {
+  if (K == 0 || ncols == 0 || K > 256 || ncols > 256) return false;
+  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 15) & ~15u;
+  return TcLayout(Kp, Np).total <= 227 * 1024;
+}
+
+int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                   const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
+                   uint64_t ldc, int* err, cudaStream_t s) {
+  if (rows == 0 || ncols == 0) return BGPU_OK;
+  BGPU_REQUIRE(gemm_tc_supported(K, ncols), BGPU_ERR_UNSUPPORTED,
+               "tensor-core rotation needs K, ncols <= 256 within shared memory");
+  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 15) & ~15u;
+  uint32_t tcols = 32;
+  while (tcols < Np) tcols <<= 1;
+  // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM
+  const size_t smem = std::max<size_t>(TcLayout(Kp, Np).total, 120 * 1024);
+  BGPU_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
+  const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)num_sms());
+  k_gemm_tc<<<grid, kTcThreads, smem, s>>>(A, lda, rows, K, Bm, ldb, ncols, C, ldc,
+                                           Kp, Np, tcols, err);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+}  // namespace bgpu

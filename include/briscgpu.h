@@ -129,8 +129,10 @@ typedef struct bgpu_solve_opts {
                                 over fixed 1024-row blocks whatever its value   */
   uint32_t reorth_passes;    /* 1 = classical Gram-Schmidt as the reference,
                                 2 = CGS2 (default when 0)                        */
-  uint32_t rotation_mode;    /* 0 = default, 1 = FP32 SIMT GEMM,
-                                2 = tcgen05 3xBF16 split GEMM                    */
+  uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor cores
+                                when subspace_size <= 112, else SIMT),
+                                1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass TF32
+                                split GEMM with FP32 accumulation                */
   volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
                                 NULL (replaces PyErr_CheckSignals, pca.pyx:1173) */
   int use_graphs;            /* replay each Lanczos step from a CUDA graph       */
@@ -194,6 +196,16 @@ BGPU_API int bgpu_irlba_f32(const float* data_matvec, const void* indices_matvec
 /* V[:, 0] of brisc/pca.pyx:801-806: `num_genes` Box-Muller normals from the
  * reference's PCG32 (cyutils.pyx:1153-1232), normalised. Host function. */
 BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_host);
+
+/* Restart rotation C = A . Bm[:, :ncols] (brisc/pca.pyx:1210-1215, the
+ * reference's matmul_nn_f_out at pca.pyx:578-616, U <- U . Ub[:, :kc]).
+ * Device pointers, all column-major: A rows x K (lda), Bm K x >= ncols (ldb),
+ * C rows x ncols (ldc). mode 1: FP32 SIMT; mode 2: tensor cores (tcgen05,
+ * 3-pass TF32 split, FP32 accumulation; K, ncols <= 112). Synchronous. */
+BGPU_API int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
+                               uint32_t K, const float* Bm, uint64_t ldb,
+                               uint32_t ncols, float* C, uint64_t ldc, int mode,
+                               void* stream);
 
 /* SVD of one m x (m+1) column-major float32 matrix B (the reference's
  * `svd(B, Ub, Sb, Vbt, ...)`, pca.pyx:531-545, JOBZ='S'). Device pointers:

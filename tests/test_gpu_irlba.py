@@ -71,12 +71,14 @@ def test_bit_identical_runs(cuda, golden):
     assert np.array_equal(a.singular_values, c.singular_values)
 
 
-@pytest.mark.parametrize("passes", [1, 2])
-def test_reorth_passes_both_meet_gates(cuda, golden, passes):
+@pytest.mark.parametrize("passes,rotation", [(1, 0), (2, 0), (2, 1), (2, 2)])
+def test_reorth_passes_both_meet_gates(cuda, golden, passes, rotation):
+    """Both Gram-Schmidt modes and both restart rotations (SIMT FP32 and the
+    tensor-core 3-pass TF32 split) meet the FP64 gates."""
     z = golden("irlba")
     X, n, g, k, m = _case(z, "clustered_b")
     M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
-    r = M.solve(k, m, reorth_passes=passes, loadings=True)
+    r = M.solve(k, m, reorth_passes=passes, rotation_mode=rotation, loadings=True)
     M.close()
     S, U, Vt = dense.top_svd(X, k + 2)
     assert r.converged
