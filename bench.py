@@ -298,11 +298,15 @@ def run_ours(args):
     # roofline: the kernel class with the most device time
     peaks = measured_peaks()
     tot = lambda key: sum(i[key] for i in infos)  # noqa: E731
+    # algorithmic bytes per launch of the sparse products: uint16 count +
+    # int32 gene index per stored entry, int32 offsets, the per-cell size
+    # factor, the dense input and output vectors
+    nnz = int(C.nnz)
+    mv_alg = nnz * 6 + (n + 1) * 4 + n * 4 + n * 4 + g * 4
+    rmv_alg = nnz * 6 + (g + 1) * 4 + n * 4 + n * 4 + g * 4
     classes = {
-        "spmv_csr (X.v)": (tot("matvec_seconds"),
-                           infos[0]["matvec_bytes"] * tot("lanczos_steps")),
-        "rmatvec_panels (X^T.u)": (tot("rmatvec_seconds"),
-                                   infos[0]["rmatvec_bytes"] * tot("rmatvecs")),
+        "spmv_csr (X.v)": (tot("matvec_seconds"), mv_alg * tot("lanczos_steps")),
+        "rmatvec_panels (X^T.u)": (tot("rmatvec_seconds"), rmv_alg * tot("rmatvecs")),
         "u_pass (dots/update)": (tot("reorth_seconds"), tot("reorth_bytes")),
         "restart_rotation": (tot("rotation_seconds"), tot("rotation_bytes")),
         "v_step": (tot("vstep_seconds"), 0.0),

@@ -113,6 +113,56 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   }
 }
 
+// CGS2 middle pass, fused: for one 256-row block, y1 = y0 - (mean + U c1)
+// (as k_uupdate) and the block's partial dots of the second pass,
+// part[b * pstride + c] = sum_r U[r, c] * y1[r], from one shared-memory copy
+// of the block's U tile (U is read once for both).
+constexpr int kFuseRows = 256;
+
+__global__ void __launch_bounds__(kFuseRows)
+k_uupdate_dots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+               const float* __restrict__ coef, const float* __restrict__ mean_sum,
+               uint64_t n, const float* __restrict__ y_in, float* __restrict__ y_out,
+               float* __restrict__ part, uint32_t pstride) {
+  extern __shared__ __align__(16) float fsm[];
+  float* us = fsm;                              // ncols x kFuseRows
+  float* cs = us + (size_t)ncols * kFuseRows;   // ncols
+  float* ys = cs + ((ncols + 3) & ~3u);         // kFuseRows
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint64_t b = blockIdx.x;
+  const uint64_t row0 = b * kFuseRows;
+  for (uint32_t c = tid; c < ncols; c += kFuseRows) cs[c] = coef[c];
+  // tile: columns of 256 rows, float4 per thread per step (rows past ldu -> 0)
+  const uint32_t q4 = kFuseRows / 4;
+  for (uint32_t t = tid; t < ncols * q4; t += kFuseRows) {
+    const uint32_t c = t / q4, r4 = (t % q4) * 4;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (row0 + r4 < ldu)
+      v = __ldcs(reinterpret_cast<const float4*>(U + (uint64_t)c * ldu + row0 + r4));
+    *reinterpret_cast<float4*>(us + (size_t)c * kFuseRows + r4) = v;
+  }
+  __syncthreads();
+  const uint64_t r = row0 + tid;
+  const float mean = mean_sum ? (*mean_sum) / (float)n : 0.f;  // pca.pyx:1025-1028
+  float y1 = 0.f;
+  if (r < n) {
+    float t = mean;
+    for (uint32_t c = 0; c < ncols; ++c) t += us[(size_t)c * kFuseRows + tid] * cs[c];
+    y1 = y_in[r] - t;
+  }
+  if (r < ldu) y_out[r] = y1;
+  ys[tid] = y1;
+  __syncthreads();
+  for (uint32_t c = wid; c < ncols; c += kFuseRows / 32) {
+    const float* uc = us + (size_t)c * kFuseRows;
+    float d = 0.f;
+#pragma unroll
+    for (int i = 0; i < kFuseRows / 32; ++i) d += uc[lane + 32 * i] * ys[lane + 32 * i];
+    d = warp_sum(d);
+    if (lane == 0) part[b * pstride + c] = d;
+  }
+}
+
 __global__ void __launch_bounds__(256)
 k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
               uint32_t ncols, float* __restrict__ out) {
@@ -384,6 +434,27 @@ int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    float* norm_part, uint32_t pstride, cudaStream_t s) {
   k_uupdate<<<(unsigned)nblocks, 256, std::max<size_t>(ncols, 1) * 4, s>>>(
       U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+size_t uupdate_dots_smem(uint32_t ncols) {
+  return ((size_t)ncols * kFuseRows + ((ncols + 3) & ~3u) + kFuseRows) * sizeof(float);
+}
+
+uint64_t uupdate_dots_blocks(uint64_t n) { return ceil_div(n, kFuseRows); }
+
+int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
+                        const float* coef, const float* mean_sum, uint64_t n,
+                        const float* y_in, float* y_out, float* part,
+                        uint32_t pstride, cudaStream_t s) {
+  const size_t smem = uupdate_dots_smem(ncols);
+  BGPU_REQUIRE(smem <= 227 * 1024, BGPU_ERR_UNSUPPORTED, "fused U pass tile too large");
+  if (smem > 48 * 1024)
+    BGPU_CUDA(cudaFuncSetAttribute(k_uupdate_dots,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_uupdate_dots<<<(unsigned)uupdate_dots_blocks(n), kFuseRows, smem, s>>>(
+      U, ldu, ncols, coef, mean_sum, n, y_in, y_out, part, pstride);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -22,6 +22,16 @@ int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    const float* y_in, float* y_out, uint64_t nblocks,
                    float* norm_part, uint32_t pstride, cudaStream_t s);
 
+// CGS2 middle pass in one read of U: y_out = y_in - (mean + U[:, :ncols] coef)
+// as launch_uupdate, and part[b * pstride + c] = U[rows of b, c] . y_out[rows
+// of b] over 256-row blocks b (uupdate_dots_blocks(n) of them).
+size_t uupdate_dots_smem(uint32_t ncols);
+uint64_t uupdate_dots_blocks(uint64_t n);
+int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
+                        const float* coef, const float* mean_sum, uint64_t n,
+                        const float* y_in, float* y_out, float* part,
+                        uint32_t pstride, cudaStream_t s);
+
 // out[c] = sum_b part[b * pstride + c] in block order (one warp per column).
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
                        uint32_t ncols, float* out, cudaStream_t s);

@@ -208,7 +208,7 @@ struct Solver {
     BGPU_TRY(balloc(Vnew, ldv * m * 4, true, s));
     BGPU_TRY(balloc(y0, ldu * 4, true, s));
     BGPU_TRY(balloc(y1, ldu * 4, true, s));
-    BGPU_TRY(balloc(part, nb * ps * 4, true, s));
+    BGPU_TRY(balloc(part, std::max<uint64_t>(nb, uupdate_dots_blocks(n)) * ps * 4, true, s));
     BGPU_TRY(balloc(coef, 2 * (size_t)ps * 4, true, s));
     BGPU_TRY(balloc(zpart, (size_t)X.num_panels * g * 4, true, s));
     BGPU_TRY(balloc(zvec, ldv * 4, true, s));
@@ -261,28 +261,32 @@ struct Solver {
       BGPU_TRY(launch_uupdate(Up, ldu, 0, coefp, coefp, n, y0p, y1p, nb, partp,
                               ps, s));
       launches += 3;
-      reorth_bytes += 3 * col;
       yfin = y1p;
     } else {
       BGPU_TRY(launch_udots(Up, ldu, j, y0p, nb, partp, ps, true, s));
       BGPU_TRY(launch_reduce_cols(partp, nb, ps, j + 1, coefp, s));
       launches += 2;
-      reorth_bytes += (j + 1) * col;
+      // algorithmic U-pass bytes (dots + update per pass): 2 n j 4 passes
+      reorth_bytes += 2.0 * j * passes * col;
       if (passes == 1) {
         BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
                                 partp, ps, s));
         launches += 1;
-        reorth_bytes += (j + 2) * col;
         yfin = y1p;
       } else {
-        BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
-                                nullptr, ps, s));
-        BGPU_TRY(launch_udots(Up, ldu, j, y1p, nb, partp, ps, false, s));
-        BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s));
+        if (uupdate_dots_smem(j) <= 227 * 1024) {
+          BGPU_TRY(launch_uupdate_dots(Up, ldu, j, coefp, coefp + j, n, y0p, y1p,
+                                       partp, ps, s));
+          BGPU_TRY(launch_reduce_cols(partp, uupdate_dots_blocks(n), ps, j, coef2, s));
+        } else {
+          BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
+                                  nullptr, ps, s));
+          BGPU_TRY(launch_udots(Up, ldu, j, y1p, nb, partp, ps, false, s));
+          BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s));
+        }
         BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y1p, y0p, nb,
                                 partp, ps, s));
         launches += 4;
-        reorth_bytes += ((j + 2) + (j + 1) + (j + 2)) * col;
         yfin = y0p;
       }
     }
@@ -305,7 +309,6 @@ struct Solver {
                           B.as<double>(), rem.as<float>(), passes, s));
     BGPU_TRY(ev_end());
     launches += 3;
-    reorth_bytes += (double)(j + 1) * g * 4.0 * 2 * passes;
     return BGPU_OK;
   }
 };

@@ -157,11 +157,13 @@ typedef struct bgpu_solve_info {
   double reorth_seconds;     /* summed U-pass time (dots, updates, norms)         */
   double vstep_seconds;      /* summed V-side step time                           */
   double rotation_seconds;   /* summed restart-rotation GEMM time                 */
-  /* Algorithmic bytes of one X.v / X^T.u launch on this layout: */
+  /* Bytes the device layout streams in one X.v / X^T.u launch (4 per
+   * stored entry in the counts layout, plus offsets, factors and vectors): */
   double matvec_bytes;
   double rmatvec_bytes;
-  double reorth_bytes;       /* summed algorithmic bytes of the U/V passes        */
-  double rotation_bytes;     /* summed algorithmic bytes of the restart rotations */
+  double reorth_bytes;       /* summed algorithmic U-pass bytes, 2 n j 4 per
+                                Gram-Schmidt pass and step                     */
+  double rotation_bytes;     /* summed (n + g)(m + kc) 4 of the restart rotations */
   uint64_t kernel_launches;  /* kernels launched by this solve                    */
 } bgpu_solve_info;
 
