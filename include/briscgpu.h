@@ -135,7 +135,8 @@ typedef struct bgpu_solve_opts {
                                 split GEMM with FP32 accumulation                */
   volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
                                 NULL (replaces PyErr_CheckSignals, pca.pyx:1173) */
-  int use_graphs;            /* replay each Lanczos step from a CUDA graph       */
+  int use_graphs;            /* reserved for CUDA-graph replay of the Lanczos
+                                steps; accepted and currently ignored            */
   int profile;               /* time the sparse products and the small SVD with
                                 CUDA events (fills the *_seconds fields)         */
   int svd_fp64;              /* small SVD in FP64 (1) or FP32 (0); B and the
