@@ -43,6 +43,10 @@ WORKLOADS = {
     # name: (cells, genes, density, k, m)
     "plain_1m": (1_000_000, 2000, 0.05, 50, 100),
     "plain_50k": (50_000, 2000, 0.08, 50, 100),
+    # 64 cell-type subsets of one shared matrix, 30 PCs each (m = 60)
+    "batched_3m": (3_000_000, 2000, 0.05, 30, 60),
+    # Poisson request stream (shapes drawn per request, see run_serve)
+    "serve": (0, 0, 0.0, 0, 0),
 }
 
 
@@ -58,6 +62,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reorth-passes", type=int, default=2)
     ap.add_argument("--sample-rows", type=int, default=125_000)
+    ap.add_argument("--concurrency", type=int, default=16,
+                    help="concurrent solves (batched_3m, serve)")
+    ap.add_argument("--subsets", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="requests/s")
+    ap.add_argument("--serve-seconds", type=float, default=15.0)
+    ap.add_argument("--serve-max-cells", type=int, default=200_000)
+    ap.add_argument("--serve-pool", type=int, default=12)
     return ap.parse_args()
 
 
@@ -367,6 +378,156 @@ def run_ours(args):
     return 0
 
 
+def subset_sizes(n: int, count: int, lo: int, hi: int, seed: int) -> np.ndarray:
+    """`count` subset sizes drawn log-uniform on [lo, hi], scaled to sum to n."""
+    rng = np.random.default_rng(seed)
+    raw = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    sizes = np.maximum(np.floor(raw * n / raw.sum()), 2).astype(np.int64)
+    sizes[np.argmax(sizes)] += n - sizes.sum()
+    return sizes
+
+
+def run_batched(args):
+    """Batched subset PCAs: one shared 3M x 2000 matrix partitioned into 64
+    cell-type subsets (sizes log-uniform on [2k, 400k]); one 30-PC IRLBA per
+    subset, each centred and scaled over its own cells. Sequential solves
+    (one at a time) against the batch (--concurrency solves in flight)."""
+    import torch
+    from brisc_gb300.batch import SharedMatrix, pca_subsets
+    torch.cuda.init()
+    C, k, m = workload(args)
+    n, g = C.num_cells, C.num_genes
+    sizes = subset_sizes(n, args.subsets, 2000, 400_000, seed=1)
+    perm = np.random.default_rng(2).permutation(n)
+    bounds = np.concatenate([[0], np.cumsum(sizes)])
+    subsets = [np.sort(perm[bounds[i]:bounds[i + 1]]) for i in range(len(sizes))]
+    S = SharedMatrix(C.indptr, C.indices, C.data, n, g, inv_size_factors=C.isf)
+    for _ in range(max(args.warmup, 1)):  # warm the kernels on the smallest subsets
+        pca_subsets(S, sorted(subsets, key=len)[:4], num_PCs=k, concurrency=4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq = pca_subsets(S, subsets, num_PCs=k, concurrency=1)
+    t_seq = time.perf_counter() - t0
+    with Clocks(0) as clk:
+        t0 = time.perf_counter()
+        bat = pca_subsets(S, subsets, num_PCs=k, concurrency=args.concurrency)
+        t_bat = time.perf_counter() - t0
+    same = all(np.array_equal(a.result.PCs, b.result.PCs) for a, b in zip(seq, bat))
+    from brisc_gb300.serve import percentile
+    lat = [r.seconds for r in bat]
+    out = {"metric": "batched subset PCAs: solves/s (64 subsets of 3M x 2000, 30 PCs)",
+           "value": len(subsets) / t_bat, "unit": "solves/s", "n_gpus": 1,
+           "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"batched_3m: {n:,} cells x {g} genes, "
+                                  f"{C.nnz:,} stored entries, {len(subsets)} subsets "
+                                  f"of {sizes.min():,}-{sizes.max():,} cells, "
+                                  f"{k} PCs, subspace {2 * k}",
+                      "concurrency": args.concurrency},
+           "sequential_solves_per_s": len(subsets) / t_seq,
+           "vs_sequential": t_seq / t_bat,
+           "batch_seconds": t_bat, "sequential_seconds": t_seq,
+           "bit_identical_to_sequential": same,
+           "subset_seconds_p50": percentile(lat, 50),
+           "subset_seconds_p99": percentile(lat, 99),
+           "converged": int(sum(r.result.converged for r in bat)),
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+    return 0
+
+
+def serve_requests(args):
+    """The request stream: Poisson arrivals at --serve-rate for --serve-seconds.
+    Each request draws cells log-uniform on [5k, --serve-max-cells], genes
+    uniform on [1k, 4k], density uniform on [3%, 8%] and 20-100 PCs; the count
+    matrices come from a pool of --serve-pool seeded matrices (host generation
+    of a fresh matrix per request would outrun the solves)."""
+    from brisc_gb300.serve import PCARequest
+    from brisc_gb300.synth import cached_nb_counts
+    rng = np.random.default_rng(11)
+    pool = []
+    for i in range(args.serve_pool):
+        cells = int(np.exp(rng.uniform(np.log(5000), np.log(args.serve_max_cells))))
+        genes = int(rng.integers(1000, 4001))
+        dens = float(rng.uniform(0.03, 0.08))
+        pool.append(cached_nb_counts(cells, genes, seed=100 + i, density=round(dens, 3)))
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_seconds:
+            break
+        arrivals.append(t)
+    # the pooled matrices live in pinned host memory, as a server's request
+    # buffers would: the uploads are then asynchronous DMA
+    import torch
+    for c in pool:
+        for name in ("indices", "data", "isf"):
+            a = getattr(c, name)
+            t = torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a)
+            pinned = t.pin_memory().numpy()
+            setattr(c, name, pinned.view(np.uint16) if a.dtype == np.uint16 else pinned)
+    reqs = []
+    for i, _ in enumerate(arrivals):
+        c = pool[i % len(pool)]
+        k = int(rng.integers(20, 101))
+        reqs.append(PCARequest(c.indptr.astype(np.int32), c.indices, c.data,
+                               c.num_genes, c.isf, num_PCs=k, seed=i, tag=i))
+    return reqs, arrivals, pool
+
+
+def run_serve(args):
+    """Served PCA requests with continuous batching (--concurrency slots,
+    admission by free HBM) against the same stream served one at a time."""
+    import torch
+    from brisc_gb300.serve import PCAServer, percentile
+    torch.cuda.init()
+    reqs, arrivals, pool = serve_requests(args)
+
+    def play(slots):
+        with PCAServer(slots=slots) as srv:
+            t0 = time.perf_counter()
+            futs = []
+            for r, a in zip(reqs, arrivals):
+                d = t0 + a - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                futs.append(srv.submit(r, arrival=t0 + a))
+            res = [f.result() for f in futs]
+            span = max(x.finish for x in res) - t0
+        errs = [x.error for x in res if x.error is not None]
+        if errs:
+            raise RuntimeError(f"{len(errs)} requests failed: {errs[0]!r}")
+        lat = [x.latency for x in res]
+        return {"solves_per_s": len(res) / span, "p50_s": percentile(lat, 50),
+                "p99_s": percentile(lat, 99), "span_s": span,
+                "max_running": srv.max_running}, res
+
+    warm = PCAServer(slots=2)
+    for f in [warm.submit(r) for r in reqs[:2]]:
+        f.result()
+    warm.close()
+    seq, _ = play(1)
+    with Clocks(0) as clk:
+        cb, res = play(args.concurrency)
+    out = {"metric": "served PCA requests: solves/s with p50/p99 latency "
+                     "(continuous batching vs one at a time)",
+           "value": cb["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+           "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"serve: Poisson {args.serve_rate}/s for "
+                                  f"{args.serve_seconds} s ({len(reqs)} requests), "
+                                  f"cells log-uniform 5k-{args.serve_max_cells:,}, "
+                                  f"genes 1k-4k, density 3-8%, 20-100 PCs, "
+                                  f"{len(pool)} pooled matrices",
+                      "slots": args.concurrency},
+           "p50_s": cb["p50_s"], "p99_s": cb["p99_s"],
+           "max_running": cb["max_running"],
+           "sequential": seq,
+           "vs_sequential": cb["solves_per_s"] / seq["solves_per_s"],
+           "converged": int(sum(x.result.converged for x in res)),
+           "clocks": clk.summary()}
+    print(json.dumps(out))
+    return 0
+
+
 def dram_traffic(kernel: str, nnz: int):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/dram_traffic.txt), scaled by stored entries to this workload."""
@@ -393,6 +554,10 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched_3m":
+        return run_batched(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

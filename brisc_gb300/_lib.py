@@ -86,6 +86,7 @@ SIGNATURES = {
     "bgpu_last_error": (C.c_char_p, []),
     "bgpu_version": (C.c_char_p, []),
     "bgpu_matrix_create": (_i, [C.POINTER(_vp), C.POINTER(MatrixDesc), _vp]),
+    "bgpu_matrix_create_rows": (_i, [C.POINTER(_vp), C.POINTER(MatrixDesc), _vp, _u64, _vp]),
     "bgpu_matrix_destroy": (_i, [_vp]),
     "bgpu_matrix_bytes": (_i, [_vp, C.POINTER(_u64)]),
     "bgpu_matrix_matvec": (_i, [_vp, _vp, _vp, _vp, _vp]),

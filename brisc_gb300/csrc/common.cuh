@@ -57,6 +57,20 @@ struct Status {
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs; refreshed at runtime
 int num_sms();                 // queried once per device
 
+// Lets `fn` use up to the device's opt-in shared memory per block. The limit
+// is a per-function setting shared by every host thread: setting it to one
+// fixed value (rather than each launch's own size) means concurrent launches
+// from several threads never meet a limit another thread has just lowered.
+int device_smem_optin();
+template <typename F>
+inline cudaError_t allow_max_smem(F* fn) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, fn);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              device_smem_optin() - (int)a.sharedSizeBytes);
+}
+
 __host__ __device__ inline uint64_t round_up(uint64_t x, uint64_t m) {
   return (x + m - 1) / m * m;
 }

@@ -451,8 +451,7 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
   const size_t smem = uupdate_dots_smem(ncols);
   BGPU_REQUIRE(smem <= 227 * 1024, BGPU_ERR_UNSUPPORTED, "fused U pass tile too large");
   if (smem > 48 * 1024)
-    BGPU_CUDA(cudaFuncSetAttribute(k_uupdate_dots,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BGPU_CUDA(allow_max_smem(k_uupdate_dots));
   k_uupdate_dots<<<(unsigned)uupdate_dots_blocks(n), kFuseRows, smem, s>>>(
       U, ldu, ncols, coef, mean_sum, n, y_in, y_out, part, pstride);
   BGPU_CHECK_LAUNCH();

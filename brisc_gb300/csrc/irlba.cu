@@ -49,6 +49,23 @@ int num_sms() {
   return cache[dev];
 }
 
+int device_smem_optin() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 227 * 1024;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (!cache[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess || v <= 0)
+      v = 227 * 1024;
+    cache[dev] = v;
+  }
+  return cache[dev];
+}
+
 // ---------------------------------------------------------------------------
 // PCG32 + Box-Muller start vector, restating brisc/cyutils.pyx:1153-1232 and
 // brisc/pca.pyx:801-806 operation for operation (float arithmetic as there).
@@ -100,18 +117,24 @@ int start_vector(uint64_t seed, uint32_t g, float* out) {
 // ---------------------------------------------------------------------------
 namespace {
 
+// Solver buffers come from the stream-ordered allocator and go back on the
+// same stream: unlike cudaMalloc/cudaFree, neither waits for the whole
+// device, so solves on different streams (batched subsets, served requests)
+// never stall one another at their start or end.
 struct Buf {
   void* p = nullptr;
+  cudaStream_t s = nullptr;
   Buf() = default;
   Buf(const Buf&) = delete;
-  ~Buf() { if (p) cudaFree(p); }
+  ~Buf() { if (p) cudaFreeAsync(p, s); }
   template <typename T>
   T* as() const { return (T*)p; }
 };
 
 int balloc(Buf& b, size_t bytes, bool zero, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(&b.p, bytes);
+  b.s = s;
+  cudaError_t e = cudaMallocAsync(&b.p, bytes, s);
   if (e != cudaSuccess) {
     b.p = nullptr;
     set_error(std::string("cudaMalloc(") + std::to_string(bytes) +
@@ -122,9 +145,9 @@ int balloc(Buf& b, size_t bytes, bool zero, cudaStream_t s) {
   return BGPU_OK;
 }
 
-struct PinnedStatus {
-  RestartStatus* h = nullptr;
-  ~PinnedStatus() { if (h) cudaFreeHost(h); }
+struct HostStatus {
+  RestartStatus v{};
+  RestartStatus* h = &v;
 };
 
 struct Solver {
@@ -143,7 +166,7 @@ struct Solver {
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
   int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
-  PinnedStatus hst;
+  HostStatus hst;
 
   // accounting
   uint64_t launches = 0;
@@ -230,7 +253,6 @@ struct Solver {
     BGPU_TRY(balloc(st, sizeof(RestartStatus), true, s));
     BGPU_TRY(balloc(sdpart, (size_t)X.num_panels * g * 16, false, s));
     BGPU_TRY(balloc(svdinfo, 16, true, s));
-    BGPU_CUDA(cudaMallocHost((void**)&hst.h, sizeof(RestartStatus)));
     return BGPU_OK;
   }
 
@@ -396,13 +418,15 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
         S.svd64 ? S.sb64.as<double>() : nullptr, m, k, S.rem.as<float>(), g,
         o.tolerance, S.smax.as<float>(), kc, S.B.as<double>(),
         S.st.as<RestartStatus>(), S.trace ? S.ratios.as<float>() : nullptr, s));
+    // restart status and the device error word in one stream round trip (no
+    // legacy-stream copies: those could wait on other streams' work)
+    int derr = 0;
     BGPU_CUDA(cudaMemcpyAsync(S.hst.h, S.st.p, sizeof(RestartStatus),
                               cudaMemcpyDeviceToHost, s));
+    BGPU_CUDA(cudaMemcpyAsync(&derr, S.derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaStreamSynchronize(s));
     BGPU_TRY(S.ev_collect());
     {
-      int derr = 0;
-      BGPU_CUDA(cudaMemcpy(&derr, S.derr.p, sizeof(int), cudaMemcpyDeviceToHost));
       BGPU_REQUIRE(derr == 0, BGPU_ERR_DEVICE,
                    "a bulk copy into shared memory did not complete within its "
                    "time limit (device error word " + std::to_string(derr) + ")");
@@ -411,8 +435,9 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     if (S.trace) {
       std::vector<float> rat(k);
       int sw[2] = {0, 0};
-      BGPU_CUDA(cudaMemcpy(rat.data(), S.ratios.p, k * 4, cudaMemcpyDeviceToHost));
-      BGPU_CUDA(cudaMemcpy(sw, S.svdinfo.p, 8, cudaMemcpyDeviceToHost));
+      BGPU_CUDA(cudaMemcpyAsync(rat.data(), S.ratios.p, k * 4, cudaMemcpyDeviceToHost, s));
+      BGPU_CUDA(cudaMemcpyAsync(sw, S.svdinfo.p, 8, cudaMemcpyDeviceToHost, s));
+      BGPU_CUDA(cudaStreamSynchronize(s));
       float worst_conv = 0.f, best_open = 1e30f;
       for (float r : rat) {
         if (r < 1.f) worst_conv = std::max(worst_conv, r);
@@ -547,6 +572,24 @@ extern "C" int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* d,
   bgpu_matrix* h = new (std::nothrow) bgpu_matrix();
   BGPU_REQUIRE(h != nullptr, BGPU_ERR_ALLOC, "host allocation failed");
   int rc = matrix_build(&h->m, d, (cudaStream_t)stream);
+  if (rc != BGPU_OK) {
+    matrix_free(&h->m);
+    delete h;
+    return rc;
+  }
+  choose_shapes(h->m);
+  *out = h;
+  return BGPU_OK;
+}
+
+extern "C" int bgpu_matrix_create_rows(bgpu_matrix** out, const bgpu_matrix_desc* d,
+                                       const int64_t* rows, uint64_t num_rows,
+                                       void* stream) {
+  BGPU_REQUIRE(out != nullptr, BGPU_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  bgpu_matrix* h = new (std::nothrow) bgpu_matrix();
+  BGPU_REQUIRE(h != nullptr, BGPU_ERR_ALLOC, "host allocation failed");
+  int rc = matrix_build_rows(&h->m, d, rows, num_rows, (cudaStream_t)stream);
   if (rc != BGPU_OK) {
     matrix_free(&h->m);
     delete h;
@@ -703,9 +746,10 @@ extern "C" int bgpu_irlba_f32(const float* data_matvec, const void* indices_matv
     BGPU_TRY(balloc(cp, (num_genes + 1) * isz, false, s));
     BGPU_TRY(balloc(ci, nnz * isz, false, s));
     BGPU_TRY(balloc(cx, nnz * 4, false, s));
-    BGPU_CUDA(cudaMemcpy(cp.p, indptr_matvec, (num_genes + 1) * isz, cudaMemcpyHostToDevice));
-    BGPU_CUDA(cudaMemcpy(ci.p, indices_matvec, nnz * isz, cudaMemcpyHostToDevice));
-    BGPU_CUDA(cudaMemcpy(cx.p, data_matvec, nnz * 4, cudaMemcpyHostToDevice));
+    BGPU_CUDA(cudaMemcpyAsync(cp.p, indptr_matvec, (num_genes + 1) * isz,
+                              cudaMemcpyHostToDevice, s));
+    BGPU_CUDA(cudaMemcpyAsync(ci.p, indices_matvec, nnz * isz, cudaMemcpyHostToDevice, s));
+    BGPU_CUDA(cudaMemcpyAsync(cx.p, data_matvec, nnz * 4, cudaMemcpyHostToDevice, s));
     BGPU_TRY(balloc(tp, (num_cells + 1) * isz, false, s));
     BGPU_TRY(balloc(ti, nnz * isz, false, s));
     BGPU_TRY(balloc(tx, nnz * 4, false, s));

@@ -23,12 +23,15 @@ enum ErrBits : int {
   kErrIndptr = 4,    // indptr decreasing or not ending at nnz
 };
 
+// Temporaries of the layout build: stream-ordered (no device-wide waits).
 struct DevBuf {
   void* p = nullptr;
-  ~DevBuf() { if (p) cudaFree(p); }
-  int alloc(size_t bytes) {
+  cudaStream_t s = nullptr;
+  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+  int alloc(size_t bytes, cudaStream_t stream) {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    s = stream;
+    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
     if (e != cudaSuccess) {
       p = nullptr;
       set_error(std::string("cudaMalloc(") + std::to_string(bytes) +
@@ -39,10 +42,13 @@ struct DevBuf {
   }
 };
 
+// Persistent matrix arrays: stream-ordered on the matrix's creation stream
+// (released on the same stream by matrix_free), so creating and destroying
+// matrices never waits for other streams' work.
 template <typename T>
-int dev_alloc(T** out, size_t count, uint64_t* bytes_acc) {
+int dev_alloc(T** out, size_t count, uint64_t* bytes_acc, cudaStream_t s) {
   size_t b = std::max<size_t>(count * sizeof(T), 16);
-  cudaError_t e = cudaMalloc((void**)out, b);
+  cudaError_t e = cudaMallocAsync((void**)out, b, s);
   if (e != cudaSuccess) {
     *out = nullptr;
     set_error(std::string("cudaMalloc(") + std::to_string(b) +
@@ -344,6 +350,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
                  "panel_rows must be a power of two in [1024, 65536]");
   }
   BGPU_CUDA(cudaGetDevice(&m->device));
+  m->stream = s;
 
   m->n = d->num_cells;
   m->g = d->num_genes;
@@ -372,12 +379,12 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     }
     BGPU_REQUIRE(first == 0 && last == (int64_t)m->nnz, BGPU_ERR_INVALID,
                  "indptr must start at 0 and end at nnz");
-    BGPU_TRY(t_indptr.alloc((m->n + 1) * isz));
+    BGPU_TRY(t_indptr.alloc((m->n + 1) * isz, s));
     BGPU_CUDA(cudaMemcpyAsync(t_indptr.p, indptr, (m->n + 1) * isz,
                               cudaMemcpyHostToDevice, s));
     indptr = t_indptr.p;
-    BGPU_TRY(t_idx.alloc(m->nnz * isz));
-    BGPU_TRY(t_val.alloc(m->nnz * vsz));
+    BGPU_TRY(t_idx.alloc(m->nnz * isz, s));
+    BGPU_TRY(t_val.alloc(m->nnz * vsz, s));
     if (m->nnz) {
       BGPU_CUDA(cudaMemcpyAsync(t_idx.p, idx, m->nnz * isz,
                                 cudaMemcpyHostToDevice, s));
@@ -387,51 +394,51 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     idx = t_idx.p;
     val = t_val.p;
     if (isf) {
-      BGPU_TRY(t_isf.alloc(m->n * 4));
+      BGPU_TRY(t_isf.alloc(m->n * 4, s));
       BGPU_CUDA(cudaMemcpyAsync(t_isf.p, isf, m->n * 4, cudaMemcpyHostToDevice, s));
       isf = (const float*)t_isf.p;
     }
     if (post && m->norm_method == BGPU_NORM_PFLOG1PPF) {
-      BGPU_TRY(t_post.alloc(m->n * 4));
+      BGPU_TRY(t_post.alloc(m->n * 4, s));
       BGPU_CUDA(cudaMemcpyAsync(t_post.p, post, m->n * 4, cudaMemcpyHostToDevice, s));
       post = (const float*)t_post.p;
     }
   }
-  BGPU_TRY(t_err.alloc(sizeof(int)));
+  BGPU_TRY(t_err.alloc(sizeof(int), s));
   int* d_err = (int*)t_err.p;
   BGPU_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), s));
 
   // Persistent arrays.
   // rowptr, isf and post carry 4 padding entries: the streaming X.v copies
   // 16-byte-aligned slices of them that may end past the last row.
-  BGPU_TRY(dev_alloc(&m->rowptr, m->n + 5, &m->bytes));
+  BGPU_TRY(dev_alloc(&m->rowptr, m->n + 5, &m->bytes, s));
   BGPU_CUDA(cudaMemsetAsync(m->rowptr, 0, (m->n + 5) * 8, s));
   if (m->mode == kFloat) {
-    BGPU_TRY(dev_alloc(&m->csr_val, m->nnz_alloc, &m->bytes));
-    BGPU_TRY(dev_alloc(&m->csr_col, m->nnz_alloc, &m->bytes));
-    BGPU_TRY(dev_alloc(&m->csc_val, m->nnz_alloc, &m->bytes));
-    BGPU_TRY(dev_alloc(&m->csc_row, m->nnz_alloc, &m->bytes));
+    BGPU_TRY(dev_alloc(&m->csr_val, m->nnz_alloc, &m->bytes, s));
+    BGPU_TRY(dev_alloc(&m->csr_col, m->nnz_alloc, &m->bytes, s));
+    BGPU_TRY(dev_alloc(&m->csc_val, m->nnz_alloc, &m->bytes, s));
+    BGPU_TRY(dev_alloc(&m->csc_row, m->nnz_alloc, &m->bytes, s));
     BGPU_CUDA(cudaMemsetAsync(m->csr_val, 0, m->nnz_alloc * 4, s));
     BGPU_CUDA(cudaMemsetAsync(m->csr_col, 0, m->nnz_alloc * 2, s));
     BGPU_CUDA(cudaMemsetAsync(m->csc_val, 0, m->nnz_alloc * 4, s));
     BGPU_CUDA(cudaMemsetAsync(m->csc_row, 0, m->nnz_alloc * 2, s));
   } else {
-    BGPU_TRY(dev_alloc(&m->csr_packed, m->nnz_alloc, &m->bytes));
-    BGPU_TRY(dev_alloc(&m->csc_packed, m->nnz_alloc, &m->bytes));
+    BGPU_TRY(dev_alloc(&m->csr_packed, m->nnz_alloc, &m->bytes, s));
+    BGPU_TRY(dev_alloc(&m->csc_packed, m->nnz_alloc, &m->bytes, s));
     BGPU_CUDA(cudaMemsetAsync(m->csr_packed, 0, m->nnz_alloc * 4, s));
     BGPU_CUDA(cudaMemsetAsync(m->csc_packed, 0, m->nnz_alloc * 4, s));
-    BGPU_TRY(dev_alloc(&m->isf, m->n + 4, &m->bytes));
+    BGPU_TRY(dev_alloc(&m->isf, m->n + 4, &m->bytes, s));
     BGPU_CUDA(cudaMemsetAsync(m->isf, 0, (m->n + 4) * 4, s));
     k_copy_float<<<grid_for(m->n, 256), 256, 0, s>>>(isf, m->isf, m->n);
     BGPU_CHECK_LAUNCH();
     if (m->norm_method == BGPU_NORM_PFLOG1PPF) {
-      BGPU_TRY(dev_alloc(&m->post, m->n + 4, &m->bytes));
+      BGPU_TRY(dev_alloc(&m->post, m->n + 4, &m->bytes, s));
       BGPU_CUDA(cudaMemsetAsync(m->post, 0, (m->n + 4) * 4, s));
       k_copy_float<<<grid_for(m->n, 256), 256, 0, s>>>(post, m->post, m->n);
       BGPU_CHECK_LAUNCH();
     }
   }
-  BGPU_TRY(dev_alloc(&m->colptr, (size_t)m->num_panels * (m->g + 1), &m->bytes));
+  BGPU_TRY(dev_alloc(&m->colptr, (size_t)m->num_panels * (m->g + 1), &m->bytes, s));
 
   // indptr is validated (and the stream synchronised) before any kernel
   // reads entries through it.
@@ -456,7 +463,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
   {
     std::vector<int64_t> rp(m->num_panels + 1);
     DevBuf t_rp;
-    BGPU_TRY(t_rp.alloc(rp.size() * 8));
+    BGPU_TRY(t_rp.alloc(rp.size() * 8, s));
     k_panel_bounds<<<grid_for(rp.size(), 256), 256, 0, s>>>(
         m->rowptr, m->n, m->pshift, m->num_panels, (int64_t*)t_rp.p);
     BGPU_CHECK_LAUNCH();
@@ -487,7 +494,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
   const uint32_t num_sub = (uint32_t)ceil_div(m->n, kSubRows);
   const uint32_t subs_per_panel = m->P / kSubRows;
   DevBuf t_cnt;
-  BGPU_TRY(t_cnt.alloc((size_t)num_sub * m->g * sizeof(int32_t)));
+  BGPU_TRY(t_cnt.alloc((size_t)num_sub * m->g * sizeof(int32_t), s));
   int32_t* cnt = (int32_t*)t_cnt.p;
   BGPU_CUDA(cudaMemsetAsync(cnt, 0, (size_t)num_sub * m->g * sizeof(int32_t), s));
   const int wblocks = (int)ceil_div(num_sub, 8);
@@ -512,13 +519,173 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
   return BGPU_OK;
 }
 
+// ===========================================================================
+// Row subsets: the layout of X[rows, :] built from a full matrix (its own
+// per-gene centring and scaling follow, since the solver computes them from
+// the matrix it is given). Device inputs are gathered on the GPU (one warp
+// per selected row); host inputs on the host.
+namespace {
+
+template <typename I>
+__global__ void k_row_lengths(const I* __restrict__ indptr, const int64_t* __restrict__ rows,
+                              uint64_t nr, uint64_t n, int64_t* __restrict__ len,
+                              int* __restrict__ err) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= nr) return;
+  const int64_t r = rows[i];
+  if (r < 0 || (uint64_t)r >= n) {
+    atomicOr(err, kErrIndptr);
+    len[i] = 0;
+    return;
+  }
+  len[i] = (int64_t)indptr[r + 1] - (int64_t)indptr[r];
+}
+
+template <typename I, typename V>
+__global__ void k_gather_rows(const I* __restrict__ indptr, const I* __restrict__ indices,
+                              const V* __restrict__ values, const int64_t* __restrict__ rows,
+                              uint64_t nr, const int64_t* __restrict__ sub_ptr,
+                              I* __restrict__ out_idx, V* __restrict__ out_val,
+                              const float* __restrict__ isf, const float* __restrict__ post,
+                              float* __restrict__ out_isf, float* __restrict__ out_post) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t i = w; i < nr; i += nw) {
+    const int64_t r = rows[i];
+    const int64_t src = (int64_t)indptr[r], dst = sub_ptr[i];
+    const int64_t len = sub_ptr[i + 1] - dst;
+    for (int64_t e = lane; e < len; e += 32) {
+      out_idx[dst + e] = indices[src + e];
+      out_val[dst + e] = values[src + e];
+    }
+    if (lane == 0) {
+      if (isf) out_isf[i] = isf[r];
+      if (post) out_post[i] = post[r];
+    }
+  }
+}
+
+template <typename I, typename V>
+int gather_device(const bgpu_matrix_desc* d, const int64_t* rows, uint64_t nr,
+                  Matrix* m, cudaStream_t s) {
+  DevBuf t_len, t_err, t_ptr, t_ptr_i, t_idx, t_val, t_isf, t_post;
+  BGPU_TRY(t_len.alloc(nr * 8, s));
+  BGPU_TRY(t_err.alloc(4, s));
+  BGPU_CUDA(cudaMemsetAsync(t_err.p, 0, 4, s));
+  k_row_lengths<I><<<grid_for(nr, 256), 256, 0, s>>>(
+      (const I*)d->indptr, rows, nr, d->num_cells, (int64_t*)t_len.p, (int*)t_err.p);
+  BGPU_CHECK_LAUNCH();
+  std::vector<int64_t> ptr(nr + 1, 0);
+  int herr = 0;
+  BGPU_CUDA(cudaMemcpyAsync(ptr.data() + 1, t_len.p, nr * 8, cudaMemcpyDeviceToHost, s));
+  BGPU_CUDA(cudaMemcpyAsync(&herr, t_err.p, 4, cudaMemcpyDeviceToHost, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  BGPU_REQUIRE(herr == 0, BGPU_ERR_INVALID, "a selected row is outside [0, num_cells)");
+  for (uint64_t i = 0; i < nr; ++i) ptr[i + 1] += ptr[i];
+  const uint64_t nnz = (uint64_t)ptr[nr];
+  BGPU_TRY(t_ptr.alloc((nr + 1) * 8, s));
+  BGPU_CUDA(cudaMemcpyAsync(t_ptr.p, ptr.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, s));
+  BGPU_TRY(t_idx.alloc(nnz * sizeof(I), s));
+  BGPU_TRY(t_val.alloc(nnz * sizeof(V), s));
+  BGPU_TRY(t_isf.alloc(nr * 4, s));
+  if (d->post_factors) BGPU_TRY(t_post.alloc(nr * 4, s));
+  const int blocks = std::max(1, (int)std::min<uint64_t>(ceil_div(nr, 8), (uint64_t)num_sms() * 16));
+  k_gather_rows<I, V><<<blocks, 256, 0, s>>>(
+      (const I*)d->indptr, (const I*)d->indices, (const V*)d->values, rows, nr,
+      (const int64_t*)t_ptr.p, (I*)t_idx.p, (V*)t_val.p, d->inv_size_factors,
+      d->post_factors, (float*)t_isf.p, (float*)t_post.p);
+  BGPU_CHECK_LAUNCH();
+  const void* sub_indptr = t_ptr.p;
+  std::vector<int32_t> ptr32;
+  if (sizeof(I) == 4) {
+    ptr32.assign(ptr.begin(), ptr.end());
+    BGPU_TRY(t_ptr_i.alloc((nr + 1) * 4, s));
+    BGPU_CUDA(cudaMemcpyAsync(t_ptr_i.p, ptr32.data(), (nr + 1) * 4,
+                              cudaMemcpyHostToDevice, s));
+    sub_indptr = t_ptr_i.p;
+  }
+  bgpu_matrix_desc sub = *d;
+  sub.indptr = sub_indptr;
+  sub.indices = t_idx.p;
+  sub.values = t_val.p;
+  sub.on_device = 1;
+  sub.num_cells = nr;
+  sub.nnz = nnz;
+  sub.inv_size_factors = d->inv_size_factors ? (const float*)t_isf.p : nullptr;
+  sub.post_factors = d->post_factors ? (const float*)t_post.p : nullptr;
+  return matrix_build(m, &sub, s);  // synchronises before the temporaries go
+}
+
+template <typename I, typename V>
+int gather_host(const bgpu_matrix_desc* d, const int64_t* rows, uint64_t nr,
+                Matrix* m, cudaStream_t s) {
+  const I* ip = (const I*)d->indptr;
+  const I* ix = (const I*)d->indices;
+  const V* vv = (const V*)d->values;
+  std::vector<I> ptr(nr + 1, 0);
+  for (uint64_t i = 0; i < nr; ++i) {
+    const int64_t r = rows[i];
+    BGPU_REQUIRE(r >= 0 && (uint64_t)r < d->num_cells, BGPU_ERR_INVALID,
+                 "a selected row is outside [0, num_cells)");
+    ptr[i + 1] = ptr[i] + (ip[r + 1] - ip[r]);
+  }
+  const uint64_t nnz = (uint64_t)ptr[nr];
+  std::vector<I> idx(nnz);
+  std::vector<V> val(nnz);
+  std::vector<float> isf(d->inv_size_factors ? nr : 0), post(d->post_factors ? nr : 0);
+  for (uint64_t i = 0; i < nr; ++i) {
+    const int64_t r = rows[i];
+    std::copy(ix + ip[r], ix + ip[r + 1], idx.begin() + ptr[i]);
+    std::copy(vv + ip[r], vv + ip[r + 1], val.begin() + ptr[i]);
+    if (d->inv_size_factors) isf[i] = d->inv_size_factors[r];
+    if (d->post_factors) post[i] = d->post_factors[r];
+  }
+  bgpu_matrix_desc sub = *d;
+  sub.indptr = ptr.data();
+  sub.indices = idx.data();
+  sub.values = val.data();
+  sub.num_cells = nr;
+  sub.nnz = nnz;
+  sub.inv_size_factors = d->inv_size_factors ? isf.data() : nullptr;
+  sub.post_factors = d->post_factors ? post.data() : nullptr;
+  return matrix_build(m, &sub, s);
+}
+
+template <typename I>
+int gather_by_value(const bgpu_matrix_desc* d, const int64_t* rows, uint64_t nr,
+                    Matrix* m, cudaStream_t s) {
+  const bool dev = d->on_device != 0;
+  if (d->value_type == BGPU_VALUE_U16)
+    return dev ? gather_device<I, uint16_t>(d, rows, nr, m, s)
+               : gather_host<I, uint16_t>(d, rows, nr, m, s);
+  return dev ? gather_device<I, uint32_t>(d, rows, nr, m, s)
+             : gather_host<I, uint32_t>(d, rows, nr, m, s);
+}
+
+}  // namespace
+
+int matrix_build_rows(Matrix* m, const bgpu_matrix_desc* d, const int64_t* rows,
+                      uint64_t nr, cudaStream_t s) {
+  BGPU_REQUIRE(d != nullptr && rows != nullptr && nr >= 1, BGPU_ERR_INVALID,
+               "desc and a non-empty row list are required");
+  BGPU_REQUIRE(d->indptr && (d->nnz == 0 || (d->indices && d->values)),
+               BGPU_ERR_INVALID, "indptr/indices/values must not be NULL");
+  BGPU_REQUIRE(d->index_type == BGPU_INDEX_I32 || d->index_type == BGPU_INDEX_I64,
+               BGPU_ERR_INVALID, "index_type must be BGPU_INDEX_I32 or _I64");
+  BGPU_REQUIRE(d->value_type >= BGPU_VALUE_U16 && d->value_type <= BGPU_VALUE_F32,
+               BGPU_ERR_INVALID, "unknown value_type");
+  return d->index_type == BGPU_INDEX_I64 ? gather_by_value<int64_t>(d, rows, nr, m, s)
+                                         : gather_by_value<int32_t>(d, rows, nr, m, s);
+}
+
 void matrix_free(Matrix* m) {
   void* ptrs[] = {m->rowptr, m->csr_packed, m->csr_val, m->csr_col,
                   m->colptr, m->csc_packed, m->csc_val, m->csc_row,
                   m->isf,    m->post,       m->sd,      m->rtab_r,
                   m->rtab_c};
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, m->stream);
   *m = Matrix();
 }
 
@@ -541,7 +708,7 @@ __global__ void k_check_indptr(const I* __restrict__ indptr, uint64_t n,
 template <typename I>
 int check_indptr(const void* indptr, uint64_t n, cudaStream_t s) {
   DevBuf e;
-  BGPU_TRY(e.alloc(sizeof(int)));
+  BGPU_TRY(e.alloc(sizeof(int), s));
   BGPU_CUDA(cudaMemsetAsync(e.p, 0, sizeof(int), s));
   k_check_indptr<I><<<grid_for(n + 1, 256), 256, 0, s>>>((const I*)indptr, n,
                                                          (int*)e.p);
@@ -685,10 +852,10 @@ int size_factors_typed(const void* indptr, const void* values, uint64_t n,
   DevBuf t_rs, t_tot, t_nrs, t_part;
   unsigned long long* rs = (unsigned long long*)row_sums_out;
   if (!rs) {
-    BGPU_TRY(t_rs.alloc(n * 8));
+    BGPU_TRY(t_rs.alloc(n * 8, s));
     rs = (unsigned long long*)t_rs.p;
   }
-  BGPU_TRY(t_tot.alloc(16));
+  BGPU_TRY(t_tot.alloc(16, s));
   unsigned long long* tot = (unsigned long long*)t_tot.p;
   BGPU_CUDA(cudaMemsetAsync(tot, 0, 16, s));
   int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(n, 8),
@@ -699,13 +866,13 @@ int size_factors_typed(const void* indptr, const void* values, uint64_t n,
   k_isf<<<grid_for(n, 256), 256, 0, s>>>(rs, n, method, tot, isf);
   BGPU_CHECK_LAUNCH();
   if (method == 2) {
-    BGPU_TRY(t_nrs.alloc(n * 4));
+    BGPU_TRY(t_nrs.alloc(n * 4, s));
     float* nrs = (float*)t_nrs.p;
     k_new_row_sums<I, V><<<blocks, 256, 0, s>>>((const I*)indptr,
                                                 (const V*)values, n, isf, nrs);
     BGPU_CHECK_LAUNCH();
     uint32_t nb = (uint32_t)ceil_div(n, 1024);
-    BGPU_TRY(t_part.alloc(nb * 4));
+    BGPU_TRY(t_part.alloc(nb * 4, s));
     k_block_float_sum<<<nb, 1024, 0, s>>>(nrs, n, qc, (float*)t_part.p);
     BGPU_CHECK_LAUNCH();
     k_post<<<grid_for(n, 256, 4096), 256, 0, s>>>((const float*)t_part.p, nb,
@@ -808,9 +975,9 @@ int csr_tocsc_typed(uint64_t n, uint32_t g, const void* Ap, const void* Aj,
                     const void* Ax, void* Bp, void* Bi, void* Bx, cudaStream_t s) {
   const uint32_t num_sub = (uint32_t)ceil_div(n, kSubRows);
   DevBuf t_cnt, t_cp, t_err;
-  BGPU_TRY(t_cnt.alloc((size_t)num_sub * g * 8));
-  BGPU_TRY(t_cp.alloc((size_t)(g + 1) * 8));
-  BGPU_TRY(t_err.alloc(4));
+  BGPU_TRY(t_cnt.alloc((size_t)num_sub * g * 8, s));
+  BGPU_TRY(t_cp.alloc((size_t)(g + 1) * 8, s));
+  BGPU_TRY(t_err.alloc(4, s));
   long long* cnt = (long long*)t_cnt.p;
   BGPU_CUDA(cudaMemsetAsync(cnt, 0, (size_t)num_sub * g * 8, s));
   BGPU_CUDA(cudaMemsetAsync(t_err.p, 0, 4, s));

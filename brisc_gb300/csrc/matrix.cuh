@@ -64,6 +64,7 @@ struct Matrix {
 
   float* sd = nullptr;  // cached clipped gene std (computed on first use)
   int device = 0;
+  cudaStream_t stream = nullptr;  // creation stream: the arrays are released on it
   uint64_t bytes = 0;
 
   // Autotuned SpMV shapes (chosen at creation from the nnz-per-row histogram).
@@ -118,6 +119,9 @@ inline CscView csc_view(const Matrix& m) {
 
 // layout.cu
 int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s);
+// The layout of X[rows, :] (rows in the memory space of d's arrays).
+int matrix_build_rows(Matrix* m, const bgpu_matrix_desc* d, const int64_t* rows,
+                      uint64_t nr, cudaStream_t s);
 void matrix_free(Matrix* m);
 
 // spmv.cu: raw products on the layout (device pointers)

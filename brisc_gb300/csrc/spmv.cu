@@ -255,15 +255,11 @@ int launch_matvec(const Matrix& m, const float* v, const float* sd, float* y,
   case GG:                                                                      \
     if (m.mode == kCounts) {                                                    \
       if (smem > 48 * 1024)                                                     \
-        BGPU_CUDA(cudaFuncSetAttribute(k_spmv<GG, kCounts>,                     \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                       (int)smem));                            \
+        BGPU_CUDA(allow_max_smem(k_spmv<GG, kCounts>));                          \
       k_spmv<GG, kCounts><<<blocks, 256, smem, s>>>(X, v, sd, y);               \
     } else {                                                                    \
       if (smem > 48 * 1024)                                                     \
-        BGPU_CUDA(cudaFuncSetAttribute(k_spmv<GG, kFloat>,                      \
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                       (int)smem));                            \
+        BGPU_CUDA(allow_max_smem(k_spmv<GG, kFloat>));                           \
       k_spmv<GG, kFloat><<<blocks, 256, smem, s>>>(X, v, sd, y);                \
     }                                                                           \
     break;
@@ -291,16 +287,12 @@ int launch_rmatvec_partials(const Matrix& m, const float* u,
   const size_t smem = (size_t)m.P * 2 * sizeof(float);
   if (m.mode == kCounts) {
     if (smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_rmat_partials<kCounts>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_rmat_partials<kCounts>));
     k_rmat_partials<kCounts><<<grid, 256, smem, s>>>(X, u, u_scale_dev, u_out,
                                                      partials, cg);
   } else {
     if (smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_rmat_partials<kFloat>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_rmat_partials<kFloat>));
     k_rmat_partials<kFloat><<<grid, 256, smem, s>>>(X, u, u_scale_dev, u_out,
                                                     partials, cg);
   }
@@ -316,15 +308,11 @@ int launch_gene_stddev(const Matrix& m, double* partials, float* sd,
   const size_t smem = (size_t)m.P * 2 * sizeof(float);
   if (m.mode == kCounts) {
     if (smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_gene_moments<kCounts>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_gene_moments<kCounts>));
     k_gene_moments<kCounts><<<grid, 256, smem, s>>>(X, (double2*)partials, cg);
   } else {
     if (smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_gene_moments<kFloat>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_gene_moments<kFloat>));
     k_gene_moments<kFloat><<<grid, 256, smem, s>>>(X, (double2*)partials, cg);
   }
   BGPU_CHECK_LAUNCH();

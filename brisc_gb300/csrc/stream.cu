@@ -627,8 +627,8 @@ int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
   if (!stream_supported(*m)) return BGPU_OK;
   const uint64_t nr = m->n * kCountTab;
   const uint64_t nc = (uint64_t)m->num_panels * kCountTab * m->P;
-  BGPU_CUDA(cudaMalloc((void**)&m->rtab_r, nr * 4));
-  BGPU_CUDA(cudaMalloc((void**)&m->rtab_c, nc * 4));
+  BGPU_CUDA(cudaMallocAsync((void**)&m->rtab_r, nr * 4, s));
+  BGPU_CUDA(cudaMallocAsync((void**)&m->rtab_c, nc * 4, s));
   *bytes_acc += (nr + nc) * 4;
   BGPU_CUDA(cudaMemsetAsync(m->rtab_c, 0, nc * 4, s));
   k_count_tables<<<(unsigned)ceil_div(nr, 256), 256, 0, s>>>(
@@ -653,8 +653,7 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
   const CsrView X = csr_view(m);
   if (m.csr_heads && m.spmv_seg) {
     const size_t smem = RowSegLayout(m.P, m.g).total;
-    BGPU_CUDA(cudaFuncSetAttribute(k_spmv_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+    BGPU_CUDA(allow_max_smem(k_spmv_seg));
     k_spmv_seg<<<m.num_panels, kSegThreads, smem, s>>>(X, m.pshift, m.rtab_c, v, sd,
                                                        y, err);
     BGPU_CHECK_LAUNCH();
@@ -662,9 +661,13 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
   }
   const size_t smem = ((size_t)((m.g + 3) & ~3u) + 32 * 2 * kTabSlot) * 4;
   if (smem > 48 * 1024)
-    BGPU_CUDA(cudaFuncSetAttribute(k_spmv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  k_spmv_rows<<<num_sms() * 4, 256, smem, s>>>(X, v, sd, y);
+    BGPU_CUDA(allow_max_smem(k_spmv_rows));
+  // one 8-lane group per row at most (32 groups per CTA): a small matrix
+  // launches a small grid and leaves the rest of the GPU to concurrent solves
+  const uint64_t want = ceil_div(m.n, 32);
+  const unsigned grid = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>(want, (uint64_t)num_sms() * 4));
+  k_spmv_rows<<<grid, 256, smem, s>>>(X, v, sd, y);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -673,8 +676,7 @@ int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
                           float* u_out, float* partT, int* err, cudaStream_t s) {
   const CscView X = csc_view(m);
   const size_t smem = SegLayout(m.P, m.g).total;
-  BGPU_CUDA(cudaFuncSetAttribute(k_rmat_seg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
+  BGPU_CUDA(allow_max_smem(k_rmat_seg));
   k_rmat_seg<<<m.num_panels, kSegThreads, smem, s>>>(X, u, u_scale, u_out, partT, err);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;

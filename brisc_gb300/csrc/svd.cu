@@ -253,17 +253,13 @@ int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
                "small SVD of this size needs a global workspace");
   if (fp64) {
     if (use_smem && smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_jacobi<double>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_jacobi<double>));
     k_jacobi<double><<<1, 1024, use_smem ? smem : 0, s>>>(
         Bd, m, Ub, Sb, Vbt, ub_last, sb64, (double*)gwork, use_smem ? 1 : 0, 40,
         1e-13, info);
   } else {
     if (use_smem && smem > 48 * 1024)
-      BGPU_CUDA(cudaFuncSetAttribute(k_jacobi<float>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+      BGPU_CUDA(allow_max_smem(k_jacobi<float>));
     k_jacobi<float><<<1, 1024, use_smem ? smem : 0, s>>>(
         Bf, m, Ub, Sb, Vbt, ub_last, sb64, (float*)gwork, use_smem ? 1 : 0, 40,
         jacobi_threshold(m), info);

@@ -256,8 +256,7 @@ int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
   while (tcols < Np) tcols <<= 1;
   // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM
   const size_t smem = std::max<size_t>(TcLayout(Kp, Np).total, 120 * 1024);
-  BGPU_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
+  BGPU_CUDA(allow_max_smem(k_gemm_tc));
   const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
   const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)num_sms());
   k_gemm_tc<<<grid, kTcThreads, smem, s>>>(A, lda, rows, K, Bm, ldb, ncols, C, ldc,

@@ -140,7 +140,10 @@ class DeviceMatrix:
     def __init__(self, indptr, indices, values, num_cells: int,
                  num_genes: int, *, norm: str | None = None,
                  inv_size_factors=None, post_factors=None,
-                 panel_rows: int = 0, stream=None):
+                 panel_rows: int = 0, stream=None, rows=None):
+        """``rows`` (int64 cell indices, NumPy for host inputs or a CUDA
+        tensor for device inputs) selects the row subset X[rows, :]: the
+        matrix is then that subset, with its own gene centring and scaling."""
         on_dev = not isinstance(indptr, np.ndarray)
         idx_dt = _np_dtype(indices)
         if idx_dt != _np_dtype(indptr) or idx_dt not in _INDEX_TYPES:
@@ -161,10 +164,24 @@ class DeviceMatrix:
         d.panel_rows = int(panel_rows)
         self._keep = (indptr, indices, values, inv_size_factors, post_factors)
         h = C.c_void_p()
-        L.call("bgpu_matrix_create", C.byref(h), C.byref(d), _stream(stream))
+        if rows is None:
+            L.call("bgpu_matrix_create", C.byref(h), C.byref(d), _stream(stream))
+            num_cells = int(num_cells)
+        else:
+            if isinstance(rows, np.ndarray):
+                if on_dev:
+                    raise TypeError("rows must be a CUDA tensor when the arrays are")
+                rows = np.ascontiguousarray(rows, dtype=np.int64)
+            elif str(rows.dtype) != "torch.int64" or not on_dev:
+                raise TypeError("rows must be int64, in the arrays' memory space")
+            L.call("bgpu_matrix_create_rows", C.byref(h), C.byref(d), _ptr(rows),
+                   int(rows.shape[0]), _stream(stream))
+            num_cells = int(rows.shape[0])
         self._h = h
         self._keep = None  # the library copied what it needs
-        self.num_cells, self.num_genes, self.nnz = int(num_cells), int(num_genes), d.nnz
+        self._stream = stream  # device memory is released on the creation stream
+        self.num_cells, self.num_genes = num_cells, int(num_genes)
+        self.nnz = int(d.nnz) if rows is None else None
         self.norm = norm
 
     @property

@@ -29,6 +29,17 @@ CHUNK = 16384
 MU_FOR_DENSITY = {0.08: -3.381, 0.05: -3.954}
 
 
+def mu_for_density(density: float) -> float:
+    """Log-mean of the per-gene means giving about `density` stored entries:
+    the two calibrated points, interpolated (and extended) linearly in
+    log(density)."""
+    if density in MU_FOR_DENSITY:
+        return MU_FOR_DENSITY[density]
+    (d0, m0), (d1, m1) = sorted(MU_FOR_DENSITY.items())
+    t = (np.log(density) - np.log(d0)) / (np.log(d1) - np.log(d0))
+    return float(m0 + t * (m1 - m0))
+
+
 @dataclass
 class CountMatrix:
     indptr: np.ndarray      # int64, n + 1
@@ -99,7 +110,7 @@ def nb_counts(num_cells: int, num_genes: int = 2000, seed: int = 0, *,
               clusters: int = 0, cluster_sigma: float = 0.8,
               workers: int | None = None) -> CountMatrix:
     if mu is None:
-        mu = MU_FOR_DENSITY.get(density, -3.954)
+        mu = mu_for_density(density)
     nchunks = (num_cells + CHUNK - 1) // CHUNK
     jobs = [(seed, ci, min(CHUNK, num_cells - ci * CHUNK), num_genes, mu,
              sigma, disp, lib_sigma, clusters, cluster_sigma)

@@ -102,6 +102,18 @@ typedef struct bgpu_matrix_desc {
 
 BGPU_API int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* desc,
                        void* stream);
+/* The layout of the row subset X[rows, :] of the matrix `desc` describes
+ * (rows: int64 cell indices, in the memory space of desc's arrays, any order,
+ * num_rows >= 1). The subset is its own matrix: a solve on it centres and
+ * scales genes over the subset's cells only, as a PCA of one cell type
+ * (SingleCell.pca() on a subset, brisc/single_cell.py:11800-11808). Used for
+ * batched per-subset PCAs over one shared matrix. */
+BGPU_API int bgpu_matrix_create_rows(bgpu_matrix** out, const bgpu_matrix_desc* desc,
+                                     const int64_t* rows, uint64_t num_rows,
+                                     void* stream);
+/* Releases the matrix's device memory, stream-ordered on the stream it was
+ * created on (that stream must still exist). Call it once no queued work uses
+ * the matrix any more (bgpu_irlba returns only after its work has completed). */
 BGPU_API int bgpu_matrix_destroy(bgpu_matrix* mat);
 /* Device bytes held by the matrix layout. */
 BGPU_API int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes);

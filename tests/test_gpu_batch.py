@@ -1,0 +1,94 @@
+"""Batched per-subset PCAs (row subsets of one resident count matrix).
+
+Each subset's PCs must be bit-identical whether solved alone from host arrays,
+sequentially from the shared device matrix, or concurrently in the batch; and
+meet the FP64 gate (relative singular-value error <= 1e-4).
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from brisc_gb300 import DeviceMatrix
+from brisc_gb300.batch import SharedMatrix, pca_subsets, subset_solve_params
+from brisc_gb300.synth import nb_counts
+from oracle import dense
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def counts():
+    c = nb_counts(12000, 400, seed=7, density=0.08, workers=1, clusters=5)
+    return c
+
+
+def _partition(n, sizes, seed=3):
+    perm = np.random.default_rng(seed).permutation(n)
+    out, at = [], 0
+    for s in sizes:
+        out.append(np.sort(perm[at:at + s]).astype(np.int64))
+        at += s
+    return out
+
+
+def test_subsets_bit_identical_alone_sequential_batched(cuda, counts):
+    c = counts
+    n, g = c.num_cells, c.num_genes
+    subsets = _partition(n, [5000, 3000, 1500, 900, 400, 150])
+    S = SharedMatrix(c.indptr, c.indices, c.data, n, g, inv_size_factors=c.isf)
+    seq = pca_subsets(S, subsets, num_PCs=12, concurrency=1)
+    bat = pca_subsets(S, subsets, num_PCs=12, concurrency=4)
+    X = c.to_scipy()
+    for rows, a, b in zip(subsets, seq, bat):
+        assert a.rows == rows.shape[0]
+        assert np.array_equal(a.result.PCs, b.result.PCs)
+        # alone, from host arrays sliced on the host
+        sub = sp.csr_matrix(X[rows])
+        sub.sort_indices()
+        k, m = subset_solve_params(rows.shape[0], g, 12, None)
+        M = DeviceMatrix(sub.indptr.astype(np.int32), sub.indices.astype(np.int32),
+                         sub.data.astype(np.uint16), rows.shape[0], g,
+                         norm="logCP10k", inv_size_factors=c.isf[rows])
+        alone = M.solve(k, m)
+        M.close()
+        assert np.array_equal(alone.PCs, a.result.PCs)
+
+
+def test_subset_meets_fp64_gate(cuda, counts):
+    c = counts
+    n, g = c.num_cells, c.num_genes
+    rows = _partition(n, [4000])[0]
+    S = SharedMatrix(c.indptr, c.indices, c.data, n, g, inv_size_factors=c.isf)
+    r = pca_subsets(S, [rows], num_PCs=10)[0].result
+    X = sp.csr_matrix(c.to_scipy()[rows])
+    rr = np.repeat(np.arange(X.shape[0]), np.diff(X.indptr))
+    Xn = sp.csr_matrix((np.log1p(X.data.astype(np.float64) * c.isf[rows][rr]),
+                        X.indices, X.indptr), shape=X.shape)
+    S64 = dense.top_svd(Xn, 12)[0]
+    assert r.converged
+    assert dense.rel_sv_error(r.PCs, S64).max() < 1e-4
+
+
+def test_host_row_subset_matches_host_slice(cuda, counts):
+    c = counts
+    n, g = c.num_cells, c.num_genes
+    rows = np.random.default_rng(5).permutation(n)[:600].astype(np.int64)  # any order
+    X = c.to_scipy()
+    sub = sp.csr_matrix(X[rows])
+    M1 = DeviceMatrix(c.indptr.astype(np.int32), c.indices, c.data, n, g,
+                      norm="logCP10k", inv_size_factors=c.isf, rows=rows)
+    M2 = DeviceMatrix(sub.indptr.astype(np.int32), sub.indices.astype(np.int32),
+                      sub.data.astype(np.uint16), rows.shape[0], g,
+                      norm="logCP10k", inv_size_factors=c.isf[rows])
+    a, b = M1.solve(8, 16), M2.solve(8, 16)
+    M1.close()
+    M2.close()
+    assert np.array_equal(a.PCs, b.PCs)
+
+
+def test_row_subset_rejects_bad_rows(cuda, counts):
+    c = counts
+    with pytest.raises(ValueError, match="outside"):
+        DeviceMatrix(c.indptr.astype(np.int32), c.indices, c.data, c.num_cells,
+                     c.num_genes, norm="logCP10k", inv_size_factors=c.isf,
+                     rows=np.array([0, c.num_cells], dtype=np.int64))
