@@ -161,7 +161,8 @@ struct Solver {
   float tol;
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
-      Vbt, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last, sb64, ratios,
+      Vbt, Ub2, Vbt2, gram, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
+      sb64, ratios,
       derr;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
   int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
@@ -242,6 +243,9 @@ struct Solver {
     BGPU_TRY(balloc(Ub, (size_t)m * m * 4, true, s));
     BGPU_TRY(balloc(Sb, (size_t)m * 4, true, s));
     BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
+    BGPU_TRY(balloc(Ub2, (size_t)m * m * 4, true, s));
+    BGPU_TRY(balloc(Vbt2, (size_t)m * (m + 1) * 4, true, s));
+    BGPU_TRY(balloc(gram, (size_t)m * m * 8, true, s));
     if (jacobi_smem_bytes(m, svd64) > 220 * 1024)
       BGPU_TRY(balloc(svdwork, jacobi_global_bytes(m, svd64), true, s));
     BGPU_TRY(balloc(ub_last, (size_t)m * 8, true, s));
@@ -409,7 +413,15 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
       BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), nullptr, m, S.Ub.as<float>(),
                                  S.Sb.as<float>(), S.Vbt.as<float>(), nullptr,
                                  nullptr, S.svdwork.p, S.svdinfo.as<int>(), s));
-      S.launches += 3;
+      // FP64-accumulated polish of the FP32 factors: Ub's columns and Vbt's
+      // rows back to orthonormal before they rotate the bases
+      BGPU_TRY(launch_orthonormalize(S.Ub.as<float>(), m, m, m, 1, S.gram.as<double>(),
+                                     S.Ub2.as<float>(), s));
+      BGPU_TRY(launch_orthonormalize(S.Vbt.as<float>(), m, m + 1, 1, m,
+                                     S.gram.as<double>(), S.Vbt2.as<float>(), s));
+      std::swap(S.Ub.p, S.Ub2.p);
+      std::swap(S.Vbt.p, S.Vbt2.p);
+      S.launches += 7;
     }
     BGPU_TRY(S.ev_end());
     BGPU_TRY(launch_restart_check(

@@ -223,7 +223,59 @@ __global__ void k_f2d(const float* __restrict__ a, uint64_t n, double* __restric
   if (i < n) b[i] = (double)a[i];
 }
 
+// One Newton-Schulz (polar) step that restores the orthonormality of the
+// FP32 small-SVD factors: for m vectors x_i of length L (element r of x_i at
+// X[i * si + r * sr]), G = (x_i . x_j) - I accumulated in FP64, then
+// x_i <- x_i - 1/2 sum_j G[i][j] x_j (FP64, rounded once to FP32). The FP32
+// Jacobi leaves the factors orthonormal only to ~1e-6; the restart rotation
+// applies them to the Lanczos bases every restart, so without this the
+// bases drift by ~1e-6 per restart.
+__global__ void __launch_bounds__(256)
+k_gram64(const float* __restrict__ X, uint32_t m, uint32_t L, uint32_t si,
+         uint32_t sr, double* __restrict__ G) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t pairs = (uint64_t)m * m;
+  if (w >= pairs) return;
+  const uint32_t i = (uint32_t)(w / m), j = (uint32_t)(w % m);
+  if (j < i) return;  // symmetric: the (j, i) warp is not needed
+  double acc = 0.0;
+  for (uint32_t r = lane; r < L; r += 32)
+    acc += (double)X[(uint64_t)i * si + (uint64_t)r * sr] *
+           (double)X[(uint64_t)j * si + (uint64_t)r * sr];
+  acc = warp_sum_t(acc);
+  if (lane == 0) {
+    const double v = acc - (i == j ? 1.0 : 0.0);
+    G[(uint64_t)i * m + j] = v;
+    G[(uint64_t)j * m + i] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_ns_update(const float* __restrict__ X, uint32_t m, uint32_t L, uint32_t si,
+            uint32_t sr, const double* __restrict__ G, float* __restrict__ Y) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)m * L) return;
+  const uint32_t i = (uint32_t)(t / L), r = (uint32_t)(t % L);
+  double acc = 0.0;
+  const double* gi = G + (uint64_t)i * m;
+  for (uint32_t j = 0; j < m; ++j) acc += gi[j] * (double)X[(uint64_t)j * si + (uint64_t)r * sr];
+  const uint64_t o = (uint64_t)i * si + (uint64_t)r * sr;
+  Y[o] = (float)((double)X[o] - 0.5 * acc);
+}
+
 }  // namespace
+
+int launch_orthonormalize(const float* X, uint32_t m, uint32_t L, uint32_t si,
+                          uint32_t sr, double* G, float* Y, cudaStream_t s) {
+  const uint64_t warps = (uint64_t)m * m;
+  k_gram64<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, s>>>(X, m, L, si, sr, G);
+  BGPU_CHECK_LAUNCH();
+  k_ns_update<<<(unsigned)ceil_div((uint64_t)m * L, 256), 256, 0, s>>>(X, m, L, si, sr,
+                                                                      G, Y);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
 
 int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s) {
   k_f2d<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(a, n, b);
