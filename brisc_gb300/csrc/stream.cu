@@ -200,7 +200,10 @@ __device__ __forceinline__ float scaled_u(const CscView& X, const float* u,
   return X.post ? uu * X.post[r] : uu;
 }
 
-__global__ void __launch_bounds__(kSegThreads, 2)
+constexpr int kRmatThreads = 384;
+constexpr int kRmatWarps = kRmatThreads / 32;
+
+__global__ void __launch_bounds__(kRmatThreads, 2)
 k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_scale,
            float* __restrict__ u_out, float* __restrict__ partT,
            int* __restrict__ err) {
@@ -226,10 +229,10 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
     bulk_g2s(smem + L.tab, X.rtab + (uint64_t)p * kCountTab * P, tb, &bar[0]);
   }
   const float scale = u_scale ? *u_scale : 1.f;
-  float usr[kMaxPanelRows / kSegThreads];
+  float usr[(kMaxPanelRows + kRmatThreads - 1) / kRmatThreads];
 #pragma unroll
-  for (int k = 0; k < kMaxPanelRows / kSegThreads; ++k) {
-    const uint32_t i = threadIdx.x + k * kSegThreads;
+  for (int k = 0; k < (kMaxPanelRows + kRmatThreads - 1) / kRmatThreads; ++k) {
+    const uint32_t i = threadIdx.x + k * kRmatThreads;
     float us = 0.f;
     if (i < rows) {
       if (u_out) u_out[r0 + i] = u_scale ? u[r0 + i] * scale : u[r0 + i];
@@ -238,12 +241,12 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
     usr[k] = us;
   }
   const int32_t* cp = X.colptr + (uint64_t)p * (X.g + 1);
-  for (uint32_t c = threadIdx.x; c <= X.g; c += kSegThreads) cps[c] = cp[c];
+  for (uint32_t c = threadIdx.x; c <= X.g; c += kRmatThreads) cps[c] = cp[c];
   __syncthreads();
 
   // Non-empty genes of the panel, in gene order.
   uint32_t S = 0;
-  for (uint32_t base = 0; base < X.g; base += kSegThreads) {
+  for (uint32_t base = 0; base < X.g; base += kRmatThreads) {
     const uint32_t c = base + threadIdx.x;
     const bool f = c < X.g && cps[c + 1] > cps[c];
     const uint32_t bal = __ballot_sync(0xffffffffu, f);
@@ -251,7 +254,7 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
     __syncthreads();
     uint32_t before = 0, tot = 0;
 #pragma unroll
-    for (int j = 0; j < kSegWarps; ++j) {
+    for (int j = 0; j < kRmatWarps; ++j) {
       const uint32_t t = (uint32_t)wtot[j];
       before += j < wid ? t : 0u;
       tot += t;
@@ -266,8 +269,8 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
   const bool ok = __syncthreads_and(mbar_wait(&bar[0], 0, err));
   if (!ok) return;  // every thread waited (bounded) for the copy
 #pragma unroll
-  for (int k = 0; k < kMaxPanelRows / kSegThreads; ++k) {
-    const uint32_t i = threadIdx.x + k * kSegThreads;
+  for (int k = 0; k < (kMaxPanelRows + kRmatThreads - 1) / kRmatThreads; ++k) {
+    const uint32_t i = threadIdx.x + k * kRmatThreads;
     if (i < P)
 #pragma unroll
       for (int c = 1; c < kCountTab; ++c) ut[c * P + i] *= usr[k];
@@ -282,12 +285,12 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
     }
     return lo;
   };
-  const uint32_t i0 = first_at((uint64_t)W * wid / kSegWarps);
-  const uint32_t i1 = wid == kSegWarps - 1 ? S : first_at((uint64_t)W * (wid + 1) / kSegWarps);
+  const uint32_t i0 = first_at((uint64_t)W * wid / kRmatWarps);
+  const uint32_t i1 = wid == kRmatWarps - 1 ? S : first_at((uint64_t)W * (wid + 1) / kRmatWarps);
   const uint32_t s0 = i0 < S ? (uint32_t)cps[nz[i0]] : W;
   const uint32_t s1 = i1 < S ? (uint32_t)cps[nz[i1]] : W;
   __syncthreads();  // cps is no longer read: its space holds the gene sums
-  for (uint32_t c = threadIdx.x; c < X.g; c += kSegThreads) gsum[c] = 0.f;
+  for (uint32_t c = threadIdx.x; c < X.g; c += kRmatThreads) gsum[c] = 0.f;
   __syncthreads();
 
   const int64_t pbase = X.rowptr[r0];
@@ -296,14 +299,27 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
   const uint32_t lt = lanemask_lt();
   float carry = 0.f;  // open segment's sum entering the next iteration
   uint32_t kb = 0;    // heads seen in earlier iterations
+  // software-pipelined: the next iteration's 32 bytes per lane are in flight
+  // while this iteration's words are summed
+  const uint4 z4 = make_uint4(0, 0, 0, 0);
+  uint4 qa = z4, qb = z4;
+  {
+    const int64_t wb0 = (beg & ~7ll) + 8 * lane;
+    if (wb0 < end) {
+      qa = ld_stream_u4(X.packed + wb0);
+      qb = ld_stream_u4(X.packed + wb0 + 4);
+    }
+  }
   for (int64_t b = beg & ~7ll; b < end; b += 256) {
     const int64_t wb = b + 8 * lane;
-    uint4 qa = make_uint4(0, 0, 0, 0), qb = qa;
-    if (wb < end) {
-      qa = ld_stream_u4(X.packed + wb);
-      qb = ld_stream_u4(X.packed + wb + 4);
+    uint4 na = z4, nb = z4;
+    if (wb + 256 < end) {
+      na = ld_stream_u4(X.packed + wb + 256);
+      nb = ld_stream_u4(X.packed + wb + 260);
     }
     uint32_t wd[8] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w};
+    qa = na;
+    qb = nb;
     if (wb < beg || wb + 8 > end) {
 #pragma unroll
       for (int i = 0; i < 8; ++i)
@@ -374,7 +390,7 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
   }
   if (lane == 0 && kb > 0) gsum[nz[i0 + kb - 1]] = carry;
   __syncthreads();
-  for (uint32_t c = threadIdx.x; c < X.g; c += kSegThreads)
+  for (uint32_t c = threadIdx.x; c < X.g; c += kRmatThreads)
     partT[(uint64_t)c * X.num_panels + p] = gsum[c];
 }
 
@@ -677,7 +693,7 @@ int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
   const CscView X = csc_view(m);
   const size_t smem = SegLayout(m.P, m.g).total;
   BGPU_CUDA(allow_max_smem(k_rmat_seg));
-  k_rmat_seg<<<m.num_panels, kSegThreads, smem, s>>>(X, u, u_scale, u_out, partT, err);
+  k_rmat_seg<<<m.num_panels, kRmatThreads, smem, s>>>(X, u, u_scale, u_out, partT, err);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

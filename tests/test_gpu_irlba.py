@@ -178,3 +178,22 @@ def test_cancel_flag(cuda, golden):
     r = M.solve(k, m)  # the context stays usable
     assert r.converged
     M.close()
+
+
+def test_large_solve_meets_fp64_gate(cuda):
+    """200k cells x 2000 genes at 5% density (the 1M workload's generator),
+    default settings (FP32 small SVD with the FP64 polish, CGS2, tensor-core
+    rotation): relative singular-value error <= 1e-4 against the FP64
+    Gram-matrix oracle, and the solve converges."""
+    from brisc_gb300.synth import nb_counts
+    c = nb_counts(200_000, 2000, seed=0, density=0.05)
+    M = DeviceMatrix(c.indptr.astype(np.int32), c.indices, c.data, c.num_cells, 2000,
+                     norm="logCP10k", inv_size_factors=c.isf)
+    r = M.solve(50, 100)
+    M.close()
+    X = c.to_scipy(np.float64)
+    rows = np.repeat(np.arange(X.shape[0]), np.diff(X.indptr))
+    X.data = np.log1p(X.data * c.isf[rows].astype(np.float64))
+    S64 = dense.top_svd(X, 52)[0]
+    assert r.converged
+    assert dense.rel_sv_error(r.PCs, S64).max() < 1e-4
