@@ -367,7 +367,7 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
     const bool tc_ok = gemm_tc_supported(o.subspace_size, o.subspace_size);
     BGPU_REQUIRE(o.rotation_mode != 2 || tc_ok, BGPU_ERR_UNSUPPORTED,
-                 "tensor-core rotation needs subspace_size <= 112");
+                 "tensor-core rotation needs subspace_size <= 104");
     S.rot_mode = o.rotation_mode == 0 ? (tc_ok ? 2 : 1) : (int)o.rotation_mode;
     const char* et = std::getenv("BGPU_TRACE");
     S.trace = et && et[0] == '1';

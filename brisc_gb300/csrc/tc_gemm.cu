@@ -11,14 +11,16 @@
 // tensor pipe carries the arithmetic (the rotation's ~25 flop/byte would need
 // ~170 TFLOP/s of FP32 to keep up with HBM).
 //
-// Shape: persistent CTAs (one per SM, 256 threads) walk 128-row tiles of U.
+// Shape: persistent CTAs (one per SM, 512 threads) walk 128-row tiles of U.
 // Ub's split halves are staged once per CTA; each tile of U is loaded with
-// coalesced 32-byte row runs, split and written in the canonical no-swizzle
-// K-major layout (8-row x 16-byte core matrices, K-direction core stride
-// LBO = 128 B, 8-row stride SBO = Kp/4 * 128 B); one elected thread issues
-// 3 * Kp/8 MMAs of M=128, N=Np, K=8 and commits them to an mbarrier; all 8
-// warps then read the accumulator back (tcgen05.ld, 32 lanes x 8 columns per
-// load) and store C column-major (128-byte runs per column).
+// coalesced 32-byte row runs into registers, split and written in the
+// canonical no-swizzle K-major layout (8-row x 16-byte core matrices,
+// K-direction core stride LBO = 128 B, 8-row stride SBO = Kp/4 * 128 B); one
+// elected thread issues 3 * Kp/8 MMAs of M=128, N=Np, K=8 and commits them to
+// an mbarrier. The next tile's loads are issued right after the MMAs, so they
+// are in flight while the MMAs run and while all 16 warps read the
+// accumulator back (tcgen05.ld, 32 lanes x 8 columns per load) and store C
+// column-major (128-byte runs per column).
 //
 // Every mbarrier wait is bounded (about 1 s of SM clock): on timeout the
 // kernel records kDevErrTimeout, stops, frees its TMEM and returns.
@@ -30,7 +32,7 @@
 namespace bgpu {
 namespace {
 
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;
 constexpr int kTcRows = 128;  // M of one MMA / rows per tile
 
 struct TcLayout {
@@ -115,6 +117,10 @@ __device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t kg, uint32_t
   return ((row >> 3) * kq + kg) * 128u + (row & 7u) * 16u;
 }
 
+// Tasks per thread when a tile's A values are staged in registers: one task
+// is 4 consecutive k of one row (128 rows x Kp/4 tasks, Kp <= 112).
+constexpr int kTcTasks = (kTcRows * 28 + kTcThreads - 1) / kTcThreads;
+
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
           const float* __restrict__ Bm, uint64_t ldb, uint32_t ncols,
@@ -127,6 +133,7 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   const TcLayout L(Kp, Np);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const uint32_t kq = Kp / 4;  // 16-byte K groups per row
+  const uint32_t ntask = kTcRows * kq;
 
   if (wid == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -158,29 +165,42 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const uint32_t idesc = idesc_tf32(kTcRows, Np);
-  const uint32_t sbo_a = kq * 128u, sbo_b = kq * 128u;
+  const uint32_t sbo = kq * 128u;
   const uint32_t base = smem_u32(smem);
 
-  const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
-  uint32_t phase = 0;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint64_t row0 = tile * kTcRows;
-    // A tile: task = (row group, k group, row in group); 8 lanes read 8
-    // consecutive rows of one column (32-byte runs).
-    for (uint32_t t = tid; t < kTcRows * kq; t += kTcThreads) {
+  // A tile values of one tile, in registers: task = (row group, k group, row
+  // in group); 8 lanes read 8 consecutive rows of one column (32-byte runs).
+  float xa[kTcTasks][4];
+  auto load_tile = [&](uint64_t row0) {
+#pragma unroll
+    for (int i = 0; i < kTcTasks; ++i) {
+      const uint32_t t = tid + i * kTcThreads;
       const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
-      const uint32_t r = rg * 8 + rr;
-      const uint64_t gr = row0 + r;
-      float x[4];
+      const uint64_t gr = row0 + rg * 8 + rr;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const uint32_t k = kg * 4 + j;
-        x[j] = (gr < rows && k < K) ? A[(uint64_t)k * lda + gr] : 0.f;
+        xa[i][j] = (t < ntask && gr < rows && k < K) ? A[(uint64_t)k * lda + gr] : 0.f;
       }
-      uint4 hi, lo;
-      split4(x, hi, lo);
-      *reinterpret_cast<uint4*>(smem + L.ahi + core_off(r, kg, kq)) = hi;
-      *reinterpret_cast<uint4*>(smem + L.alo + core_off(r, kg, kq)) = lo;
+    }
+  };
+
+  const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
+  uint32_t phase = 0;
+  uint64_t tile = blockIdx.x;
+  if (tile < ntiles) load_tile(tile * kTcRows);
+  for (; tile < ntiles; tile += gridDim.x) {
+    const uint64_t row0 = tile * kTcRows;
+#pragma unroll
+    for (int i = 0; i < kTcTasks; ++i) {
+      const uint32_t t = tid + i * kTcThreads;
+      if (t < ntask) {
+        const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
+        uint4 hi, lo;
+        split4(xa[i], hi, lo);
+        *reinterpret_cast<uint4*>(smem + L.ahi + core_off(rg * 8 + rr, kg, kq)) = hi;
+        *reinterpret_cast<uint4*>(smem + L.alo + core_off(rg * 8 + rr, kg, kq)) = lo;
+      }
     }
     fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
     tc_fence_before();
@@ -189,16 +209,18 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
       tc_fence_after();
       for (uint32_t ks = 0; ks < Kp / 8; ++ks) {
         const uint32_t off = ks * 256u;  // two 16-byte K groups per K=8 step
-        const uint64_t ah = smem_desc(base + L.ahi + off, 128u, sbo_a);
-        const uint64_t al = smem_desc(base + L.alo + off, 128u, sbo_a);
-        const uint64_t bh = smem_desc(base + L.bhi + off, 128u, sbo_b);
-        const uint64_t bl = smem_desc(base + L.blo + off, 128u, sbo_b);
+        const uint64_t ah = smem_desc(base + L.ahi + off, 128u, sbo);
+        const uint64_t al = smem_desc(base + L.alo + off, 128u, sbo);
+        const uint64_t bh = smem_desc(base + L.bhi + off, 128u, sbo);
+        const uint64_t bl = smem_desc(base + L.blo + off, 128u, sbo);
         mma_tf32(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
         mma_tf32(tmem, ah, bl, idesc, 1u);
         mma_tf32(tmem, al, bh, idesc, 1u);
       }
       mma_commit(bar);
     }
+    // the next tile's loads fly while the MMAs run and the accumulator drains
+    if (tile + gridDim.x < ntiles) load_tile((tile + gridDim.x) * kTcRows);
     const bool ok = mbar_wait(bar, phase, err);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) stop = 1;
@@ -206,12 +228,12 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     }
     phase ^= 1u;
     tc_fence_after();
-    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (tile rows), columns of
-    // its half; lane = row.
+    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (tile rows) and the
+    // columns of quarter w/4; lane = row.
     const uint32_t q = wid & 3u, h = wid >> 2;
-    const uint32_t half = Np / 2;
+    const uint32_t quarter = Np / 4;
     const uint64_t gr = row0 + q * 32 + lane;
-    for (uint32_t c0 = h * half; c0 < (h + 1) * half; c0 += 8) {
+    for (uint32_t c0 = h * quarter; c0 < (h + 1) * quarter; c0 += 8) {
       float v[8];
       tmem_ld8(tmem + ((q * 32u) << 16) + c0, v);
       if (gr < rows) {
@@ -240,8 +262,8 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
 }  // namespace
 
 bool gemm_tc_supported(uint32_t K, uint32_t ncols) {
-  if (K == 0 || ncols == 0 || K > 256 || ncols > 256) return false;
-  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 15) & ~15u;
+  if (K == 0 || ncols == 0 || K > 112 || ncols > 256) return false;
+  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 31) & ~31u;
   return TcLayout(Kp, Np).total <= 227 * 1024;
 }
 
@@ -251,7 +273,7 @@ int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
   if (rows == 0 || ncols == 0) return BGPU_OK;
   BGPU_REQUIRE(gemm_tc_supported(K, ncols), BGPU_ERR_UNSUPPORTED,
                "tensor-core rotation needs K, ncols <= 256 within shared memory");
-  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 15) & ~15u;
+  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 31) & ~31u;
   uint32_t tcols = 32;
   while (tcols < Np) tcols <<= 1;
   // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM

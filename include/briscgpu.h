@@ -142,7 +142,7 @@ typedef struct bgpu_solve_opts {
   uint32_t reorth_passes;    /* 1 = classical Gram-Schmidt as the reference,
                                 2 = CGS2 (default when 0)                        */
   uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor cores
-                                when subspace_size <= 112, else SIMT),
+                                when subspace_size <= 104, else SIMT),
                                 1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass TF32
                                 split GEMM with FP32 accumulation                */
   volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
@@ -216,7 +216,7 @@ BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_hos
  * reference's matmul_nn_f_out at pca.pyx:578-616, U <- U . Ub[:, :kc]).
  * Device pointers, all column-major: A rows x K (lda), Bm K x >= ncols (ldb),
  * C rows x ncols (ldc). mode 1: FP32 SIMT; mode 2: tensor cores (tcgen05,
- * 3-pass TF32 split, FP32 accumulation; K, ncols <= 112). Synchronous. */
+ * 3-pass TF32 split, FP32 accumulation; K, ncols <= 104). Synchronous. */
 BGPU_API int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
                                uint32_t K, const float* Bm, uint64_t ldb,
                                uint32_t ncols, float* C, uint64_t ldc, int mode,
