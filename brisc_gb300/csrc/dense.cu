@@ -10,6 +10,7 @@
 #include <cooperative_groups.h>
 
 #include "dense.cuh"
+#include "tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -132,15 +133,22 @@ k_uupdate_dots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   const uint64_t b = blockIdx.x;
   const uint64_t row0 = b * kFuseRows;
   for (uint32_t c = tid; c < ncols; c += kFuseRows) cs[c] = coef[c];
-  // tile: columns of 256 rows, float4 per thread per step (rows past ldu -> 0)
+  // tile: columns of 256 rows by asynchronous 16-byte global -> shared copies
+  // (cp.async: every copy of the tile is in flight at once, no register
+  // staging); rows past ldu are zero-filled
   const uint32_t q4 = kFuseRows / 4;
   for (uint32_t t = tid; t < ncols * q4; t += kFuseRows) {
     const uint32_t c = t / q4, r4 = (t % q4) * 4;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (row0 + r4 < ldu)
-      v = __ldcs(reinterpret_cast<const float4*>(U + (uint64_t)c * ldu + row0 + r4));
-    *reinterpret_cast<float4*>(us + (size_t)c * kFuseRows + r4) = v;
+    float* dst = us + (size_t)c * kFuseRows + r4;
+    if (row0 + r4 < ldu) {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)),
+                   "l"(U + (uint64_t)c * ldu + row0 + r4)
+                   : "memory");
+    } else {
+      *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
   }
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   const uint64_t r = row0 + tid;
   const float mean = mean_sum ? (*mean_sum) / (float)n : 0.f;  // pca.pyx:1025-1028
