@@ -21,17 +21,40 @@ namespace {
 
 __device__ __forceinline__ void pair_of(int round, int idx, int M2, int* p,
                                         int* q) {
-  const int L = M2 - 1;
+  const int L = M2 - 1;  // round, idx < L: one conditional subtraction is the modulo
   int a, b;
   if (idx == 0) {
     a = round;
     b = L;
   } else {
-    a = (round + idx) % L;
-    b = (round - idx + L) % L;
+    a = round + idx;
+    a -= a >= L ? L : 0;
+    b = round - idx + L;
+    b -= b >= L ? L : 0;
   }
   *p = min(a, b);
   *q = max(a, b);
+}
+
+// Jacobi rotation (c, s) zeroing the off-diagonal ga of the Gram block
+// [al ga; ga be]: with x = be - al, y = 2 ga, t = tan(theta) =
+// sign(x y) |y| / (|x| + sqrt(x^2 + y^2)) (the smaller root, no cancellation),
+// c = 1 / sqrt(1 + t^2), s = c t. Every operation is correctly rounded.
+__device__ __forceinline__ void rotation_of(float al, float be, float ga, float* c,
+                                            float* s) {
+  const float x = be - al, y = 2.f * ga;
+  const float r = sqrtf(fmaf(x, x, y * y));
+  const float t = copysignf(fabsf(y), x * y) / (fabsf(x) + r);
+  *c = __frsqrt_rn(fmaf(t, t, 1.f));
+  *s = *c * t;
+}
+__device__ __forceinline__ void rotation_of(double al, double be, double ga, double* c,
+                                            double* s) {
+  const double x = be - al, y = 2.0 * ga;
+  const double r = sqrt(fma(x, x, y * y));
+  const double t = copysign(fabs(y), x * y) / (fabs(x) + r);
+  *c = 1.0 / sqrt(fma(t, t, 1.0));
+  *s = *c * t;
 }
 
 template <typename T>
@@ -97,11 +120,9 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
           be += __shfl_xor_sync(gm8, be, o);
           ga += __shfl_xor_sync(gm8, ga, o);
         }
-        if (al > T(0) && be > T(0) && fabs(ga) > thresh * sqrt(al * be)) {
-          const T zeta = (be - al) / (T(2) * ga);
-          const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-          const T c = T(1) / sqrt(T(1) + t * t);
-          const T sn = c * t;
+        if (al > T(0) && be > T(0) && ga * ga > thresh * thresh * (al * be)) {
+          T c, sn;
+          rotation_of(al, be, ga, &c, &sn);
           for (int r = l8; r < la; r += 8) {
             const T x = ap[r], y = aq[r];
             ap[r] = c * x - sn * y;
