@@ -72,6 +72,21 @@ def parse():
     return ap.parse_args()
 
 
+def reduce_replicas(seconds_or_ms: float, launches: float, device):
+    """Across the ranks of a replica run: the largest time (the job ends when
+    the slowest replica does) and the summed kernel launches. One rank (or no
+    process group): the values themselves."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(seconds_or_ms), float(launches)
+    t = torch.tensor([seconds_or_ms], dtype=torch.float64, device=device)
+    n = torch.tensor([launches], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n)
+    return float(t.item()), float(n.item())
+
+
 def dist_init(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -263,14 +278,8 @@ def run_ours(args):
         barrier()
     ms = start.elapsed_time(stop)
     clocks = clk.summary()
-    ms_t = torch.tensor([ms], device=dev)
-    launches = torch.tensor([sum(i["kernel_launches"] for i in infos)], device=dev,
-                            dtype=torch.float64)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(launches)
-    ms_max = float(ms_t.item())
+    ms_max, launch_total = reduce_replicas(
+        ms, float(sum(i["kernel_launches"] for i in infos)), dev)
     value = ms_max / 1e3 / (args.steps * ws)
     last = r
     M.close()
@@ -298,11 +307,8 @@ def run_ours(args):
         Me.close()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0)
-    e2e_t = torch.tensor([e2e_s], device=dev)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = float(e2e_t.item()) / (e2e_steps * ws)
+    e2e_max, _ = reduce_replicas(e2e_s, 0.0, dev)
+    e2e_value = e2e_max / (e2e_steps * ws)
 
     if rank != 0:
         return 0
@@ -369,7 +375,7 @@ def run_ours(args):
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h},
            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-           "gpu_launches": int(launches.item()),
+           "gpu_launches": int(launch_total),
            "solve": {"restarts": last.info["restarts"],
                      "lanczos_steps": last.info["lanczos_steps"],
                      "converged": last.converged,
