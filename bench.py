@@ -333,7 +333,8 @@ def run_ours(args):
     # path's bandwidth-bound kernels); the other classes go into time_share
     avg_row = nnz / max(n, 1)
     kern = {"spmv_csr (X.v)": "k_spmv_rows" if avg_row >= 64 else "k_spmv_seg",
-            "rmatvec_panels (X^T.u)": "k_rmat_seg"}
+            # the compact 16-bit panel copy serves X^T.u for up to 2048 genes
+            "rmatvec_panels (X^T.u)": "k_rmat_seg16" if g <= 2048 else "k_rmat_seg"}
     dominant = max(kern, key=lambda c: classes[c][0])
     secs, byts = classes[dominant]
     launches_dom = tot("lanczos_steps") if dominant.startswith("spmv") else tot("rmatvecs")

@@ -14,6 +14,9 @@
 //                                          (panel, gene) segment
 //     rtab_c      float32[panels*16*P]    per panel, [count][row] table of
 //                                          log1pf(count * isf) (count 0 -> 0)
+//     csc16       uint16[nnz16]           compact panel copy (g <= 2048, P =
+//                                          1024): head << 15 | row << 5 | code,
+//                                          code = count (0-15) or 16 (>= 16)
 //     isf, post   float32[n]              per-cell factors (post may be null)
 //   kFloat mode (pre-normalised values, 6 bytes per stored entry):
 //     csr_val float32[nnz4], csr_col uint16[nnz4]
@@ -61,6 +64,7 @@ struct Matrix {
   float* post = nullptr;
   float* rtab_r = nullptr;  // [cell][kCountTab] (X.v)
   float* rtab_c = nullptr;  // [panel][kCountTab][P] (X^T.u)
+  uint16_t* csc16 = nullptr;  // compact panel entries (stream16.cu)
 
   float* sd = nullptr;  // cached clipped gene std (computed on first use)
   int device = 0;
@@ -75,6 +79,7 @@ struct Matrix {
   // Table-driven products (stream.cu) for the counts layout.
   bool stream_ok = false;  // count tables built; the table-driven kernels apply
   bool csr_heads = false;  // CSR words carry row-head flags (segmented X.v)
+  bool compact = false;    // 16-bit panel copy built: X^T.u uses it
   bool spmv_seg = false;   // X.v by the segmented stream (short rows) rather
                            // than 8 lanes per row
   int impl = 0;            // 0 = table-driven kernels, 1 = register-vector kernels
@@ -149,6 +154,12 @@ int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
                           float* u_out, float* partT, int* err, cudaStream_t s);
 int launch_reduce_panels_t(const Matrix& m, const float* partT, const float* sd,
                            float* z, cudaStream_t s);
+
+// stream16.cu: X^T.u on the compact 16-bit panel entries.
+bool compact16_supported(const Matrix& m);
+int build_compact16(Matrix* m, cudaStream_t s, uint64_t* bytes_acc);
+int launch_rmatvec16(const Matrix& m, const float* u, const float* u_scale,
+                     float* u_out, float* partT, int* err, cudaStream_t s);
 
 // Bytes of the algorithmic traffic of one X.v / X^T.u launch (used for the
 // roofline figure). Counts what the chosen layout must stream.

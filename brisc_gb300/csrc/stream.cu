@@ -25,6 +25,7 @@
 // result depends only on the data and the layout, not on timing or launch
 // shape, so repeated products are bit-identical.
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "matrix.cuh"
@@ -661,6 +662,9 @@ int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
     BGPU_CHECK_LAUNCH();
   }
   m->stream_ok = true;
+  // BGPU_COMPACT=0 keeps X^T.u on the 32-bit panel words (A/B study)
+  const char* ec = std::getenv("BGPU_COMPACT");
+  if (!(ec && ec[0] == '0')) BGPU_TRY(build_compact16(m, s, bytes_acc));
   return BGPU_OK;
 }
 
@@ -690,6 +694,7 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
 
 int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
                           float* u_out, float* partT, int* err, cudaStream_t s) {
+  if (m.compact) return launch_rmatvec16(m, u, u_scale, u_out, partT, err, s);
   const CscView X = csc_view(m);
   const size_t smem = SegLayout(m.P, m.g).total;
   BGPU_CUDA(allow_max_smem(k_rmat_seg));
