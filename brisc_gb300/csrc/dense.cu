@@ -171,16 +171,26 @@ k_uupdate_dots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   }
 }
 
-__global__ void __launch_bounds__(256)
+// out[c] = sum over blocks b of part[b * pstride + c]. A CTA owns 32 columns
+// (lane = column, so every load is one coalesced 128-byte row run); its 32
+// warps take blocks b = w, w + 32, ... and the 32 warp sums are added in warp
+// order, a fixed order whatever the timing.
+__global__ void __launch_bounds__(1024)
 k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
               uint32_t ncols, float* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (c >= ncols) return;
+  __shared__ float ws[32][33];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.x * 32 + lane;
   float t = 0.f;
-  for (uint64_t b = lane; b < nblocks; b += 32) t += part[b * pstride + c];
-  t = warp_sum(t);
-  if (lane == 0) out[c] = t;
+  if (c < ncols)
+    for (uint64_t b = wid; b < nblocks; b += 32) t += part[b * pstride + c];
+  ws[wid][lane] = t;
+  __syncthreads();
+  if (wid == 0 && c < ncols) {
+    float r = 0.f;
+    for (int w = 0; w < 32; ++w) r += ws[w][lane];
+    out[c] = r;
+  }
 }
 
 __global__ void __launch_bounds__(256)
@@ -469,8 +479,8 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
                        uint32_t ncols, float* out, cudaStream_t s) {
   if (ncols == 0) return BGPU_OK;
-  k_reduce_cols<<<(unsigned)ceil_div(ncols, 8), 256, 0, s>>>(part, nblocks,
-                                                             pstride, ncols, out);
+  k_reduce_cols<<<(unsigned)ceil_div(ncols, 32), 1024, 0, s>>>(part, nblocks,
+                                                               pstride, ncols, out);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

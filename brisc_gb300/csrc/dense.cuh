@@ -32,7 +32,8 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
                         const float* y_in, float* y_out, float* part,
                         uint32_t pstride, cudaStream_t s);
 
-// out[c] = sum_b part[b * pstride + c] in block order (one warp per column).
+// out[c] = sum_b part[b * pstride + c] (coalesced: lanes take columns, warps
+// stride the blocks; the warp sums are added in warp order).
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
                        uint32_t ncols, float* out, cudaStream_t s);
 

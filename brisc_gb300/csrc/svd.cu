@@ -41,20 +41,22 @@ __device__ __forceinline__ void pair_of(int round, int idx, int M2, int* p,
 // sign(x y) |y| / (|x| + sqrt(x^2 + y^2)) (the smaller root, no cancellation),
 // c = 1 / sqrt(1 + t^2), s = c t. Every operation is correctly rounded.
 __device__ __forceinline__ void rotation_of(float al, float be, float ga, float* c,
-                                            float* s) {
+                                            float* s, float* tan_out) {
   const float x = be - al, y = 2.f * ga;
   const float r = sqrtf(fmaf(x, x, y * y));
   const float t = copysignf(fabsf(y), x * y) / (fabsf(x) + r);
   *c = __frsqrt_rn(fmaf(t, t, 1.f));
   *s = *c * t;
+  *tan_out = t;
 }
 __device__ __forceinline__ void rotation_of(double al, double be, double ga, double* c,
-                                            double* s) {
+                                            double* s, double* tan_out) {
   const double x = be - al, y = 2.0 * ga;
   const double r = sqrt(fma(x, x, y * y));
   const double t = copysign(fabs(y), x * y) / (fabs(x) + r);
   *c = 1.0 / sqrt(fma(t, t, 1.0));
   *s = *c * t;
+  *tan_out = t;
 }
 
 template <typename T>
@@ -96,9 +98,21 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
   const int l8 = threadIdx.x & 7;
   const unsigned gm8 = 0xFFu << (lane & 24);
   const int grp = threadIdx.x >> 3, ngrp = blockDim.x >> 3;
+  // Squared column norms live in `sig` during the sweeps: recomputed at each
+  // sweep's start and carried through the rotations by the exact identities
+  // |a_p'|^2 = |a_p|^2 - t ga, |a_q'|^2 = |a_q|^2 + t ga, so a pair needs only
+  // its cross product.
+  T* nrm = sig;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) rotated = 0;
+    for (uint32_t i = wid; i < m; i += nw) {
+      const T* ai = A + (uint64_t)i * la;
+      T t2 = 0;
+      for (int r = lane; r < la; r += 32) t2 += ai[r] * ai[r];
+      t2 = warp_sum_t(t2);
+      if (lane == 0) nrm[i] = t2;
+    }
     __syncthreads();
     for (int round = 0; round < M2 - 1; ++round) {
       for (int idx = grp; idx < M2 / 2; idx += ngrp) {
@@ -107,22 +121,18 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
         if (q >= (int)m) continue;
         T* ap = A + (uint64_t)p * la;
         T* aq = A + (uint64_t)q * la;
-        T al = 0, be = 0, ga = 0;
-        for (int r = l8; r < la; r += 8) {
-          const T x = ap[r], y = aq[r];
-          al += x * x;
-          be += y * y;
-          ga += x * y;
-        }
+        const T al = nrm[p], be = nrm[q];
+        T ga = 0;
+        for (int r = l8; r < la; r += 8) ga += ap[r] * aq[r];
 #pragma unroll
-        for (int o = 4; o > 0; o >>= 1) {
-          al += __shfl_xor_sync(gm8, al, o);
-          be += __shfl_xor_sync(gm8, be, o);
-          ga += __shfl_xor_sync(gm8, ga, o);
-        }
+        for (int o = 4; o > 0; o >>= 1) ga += __shfl_xor_sync(gm8, ga, o);
         if (al > T(0) && be > T(0) && ga * ga > thresh * thresh * (al * be)) {
-          T c, sn;
-          rotation_of(al, be, ga, &c, &sn);
+          T c, sn, tn;
+          rotation_of(al, be, ga, &c, &sn, &tn);
+          if (l8 == 0) {
+            nrm[p] = al - tn * ga;
+            nrm[q] = be + tn * ga;
+          }
           for (int r = l8; r < la; r += 8) {
             const T x = ap[r], y = aq[r];
             ap[r] = c * x - sn * y;
