@@ -43,6 +43,8 @@ WORKLOADS = {
     # name: (cells, genes, density, k, m)
     "plain_1m": (1_000_000, 2000, 0.05, 50, 100),
     "plain_50k": (50_000, 2000, 0.08, 50, 100),
+    # the large solve: ~1B stored entries (int64 offsets), 100 PCs
+    "large_10m": (10_000_000, 2000, 0.05, 100, 200),
     # 64 cell-type subsets of one shared matrix, 30 PCs each (m = 60)
     "batched_3m": (3_000_000, 2000, 0.05, 30, 60),
     # Poisson request stream (shapes drawn per request, see run_serve)
@@ -233,7 +235,8 @@ def config_of(args, C, k, m):
                         f"fused",
             "cells": C.num_cells, "genes": C.num_genes, "nnz": C.nnz,
             "num_PCs": k, "subspace_size": m, "value_dtype": "uint16",
-            "index_dtype": "int32", "l2": "inputs larger than L2 (no flush)",
+            "index_dtype": "int64" if C.nnz >= 2 ** 31 else "int32",
+            "l2": "inputs larger than L2 (no flush)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -254,9 +257,11 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    # resident matrix (int32 indptr: nnz < 2^31 at this size)
-    ip32 = C.indptr.astype(np.int32)
-    M = DeviceMatrix(ip32, C.indices, C.data, n, g, norm="logCP10k",
+    # resident matrix (int32 offsets while nnz < 2^31, else int64)
+    wide = C.nnz >= 2 ** 31
+    ip32 = C.indptr if wide else C.indptr.astype(np.int32)
+    idx = C.indices.astype(np.int64) if wide else C.indices
+    M = DeviceMatrix(ip32, idx, C.data, n, g, norm="logCP10k",
                      inv_size_factors=C.isf, stream=stream)
     pcs_dev = torch.empty((n, k), dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -287,7 +292,7 @@ def run_ours(args):
     # end-to-end through the C ABI with pinned host buffers
     e2e_steps = args.e2e_steps or min(3, args.steps)
     h_ip = torch.from_numpy(ip32).pin_memory()
-    h_ix = torch.from_numpy(C.indices).pin_memory()
+    h_ix = torch.from_numpy(idx).pin_memory()
     h_v = torch.from_numpy(C.data.view(np.int16)).pin_memory()
     h_sf = torch.from_numpy(C.isf).pin_memory()
     h_pcs = torch.empty((n, k), dtype=torch.float32).pin_memory()
