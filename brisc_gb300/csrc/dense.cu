@@ -271,7 +271,8 @@ k_vstep(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
 // memory, every CTA summing the 8 partials in rank order (so all CTAs hold
 // the same bits and the result does not depend on timing).
 constexpr int kVCluster = 8;
-constexpr int kVThreads = 256;
+constexpr int kVThreads = 1024;
+constexpr int kVSplit = 4;  // threads sharing one gene's update sum
 
 __global__ void __cluster_dims__(kVCluster, 1, 1) __launch_bounds__(kVThreads)
 k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
@@ -283,6 +284,7 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
   float* zs = vsm;                            // slice
   float* pd = zs + ((slice + 3) & ~3u);       // 2 x m partial dots (per pass)
   float* dots = pd + 2 * m;                   // m
+  float* upd = dots + ((m + 3) & ~3u);        // kVSplit x slice partial updates
   __shared__ double pn;                       // partial squared norm
   __shared__ double wred[kVThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -309,10 +311,23 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
       dots[col] = t;
     }
     __syncthreads();
+    // each gene's sum over columns split in kVSplit fixed strands (col = h,
+    // h + kVSplit, ...), added in strand order
+    for (uint32_t t = threadIdx.x; t < kVSplit * slice; t += kVThreads) {
+      const uint32_t h = t / slice, c = c0 + t % slice;
+      float acc = 0.f;
+      if (c < c1)
+        for (uint32_t col = h; col <= j; col += kVSplit)
+          acc += V[c + (uint64_t)col * ldv] * dots[col];
+      upd[t] = acc;
+    }
+    __syncthreads();
     for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads) {
+      const uint32_t i = c - c0;
       float t = 0.f;
-      for (uint32_t col = 0; col <= j; ++col) t += V[c + (uint64_t)col * ldv] * dots[col];
-      zs[c - c0] -= t;
+#pragma unroll
+      for (int h = 0; h < kVSplit; ++h) t += upd[h * slice + i];
+      zs[i] -= t;
     }
     __syncthreads();
   }
@@ -497,7 +512,8 @@ int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
                  uint32_t j, uint32_t m, const float* scal, double* B,
                  float* rem, int passes, cudaStream_t s) {
   const uint32_t slice = (g + kVCluster - 1) / kVCluster;
-  const size_t csm = ((size_t)((slice + 3) & ~3u) + 3ull * m) * sizeof(float);
+  const size_t csm = ((size_t)((slice + 3) & ~3u) + 2ull * m + ((m + 3) & ~3u) +
+                      (size_t)kVSplit * slice) * sizeof(float);
   if (csm <= 48 * 1024) {
     k_vstep_cluster<<<kVCluster, kVThreads, csm, s>>>(z, V, ldv, g, j, m, scal, B,
                                                      rem, passes);

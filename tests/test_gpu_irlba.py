@@ -57,6 +57,29 @@ def test_dropin_irlba_matches_reference(cuda, golden, name):
     assert dense.max_angle(PCs[:, :j], U[:, :j]) < 1e-3
 
 
+def test_dropin_csc_input_matches_csr_input(cuda, golden):
+    """is_csr=False (the matvec arrays hold a CSC copy, as the reference's
+    single-thread CSC path passes them) gives the CSR call's PCs bit for bit:
+    the GPU transpose restores the same sorted CSR layout."""
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_b")
+    X.sort_indices()
+    csc = X.tocsc()
+    csc.sort_indices()
+    out = []
+    for is_csr in (True, False):
+        PCs = np.empty((n, k), dtype=np.float32)
+        mv, rmv = (X, csc) if is_csr else (csc, X)
+        bg.irlba(data_matvec=mv.data, indices_matvec=mv.indices, indptr_matvec=mv.indptr,
+                 data_rmatvec=rmv.data, indices_rmatvec=rmv.indices,
+                 indptr_rmatvec=rmv.indptr, num_cells=n, num_genes=g, k=k,
+                 subspace_size=m, tolerance=1e-6, max_iterations=100, seed=0,
+                 match_parallel=False, is_csr=is_csr, num_threads=1,
+                 chunk_size=1024, PCs=PCs)
+        out.append(PCs)
+    assert np.array_equal(out[0], out[1])
+
+
 def test_bit_identical_runs(cuda, golden):
     z = golden("irlba")
     X, n, g, k, m = _case(z, "clustered_a")
