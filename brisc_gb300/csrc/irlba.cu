@@ -172,46 +172,53 @@ struct Solver {
   // accounting
   uint64_t launches = 0;
   double reorth_bytes = 0, rotation_bytes = 0;
-  // profiling: event pairs around the sparse products and the small SVD
+  // profiling: event pairs around each kernel class, in two pools that
+  // alternate by restart: a restart's events are read on the host while the
+  // GPU runs the next rotation, not while it waits at the restart's sync
   bool profile = false;
-  std::vector<cudaEvent_t> ev;
+  std::vector<cudaEvent_t> ev[2];
   // kinds: 0 X.v, 1 X^T.u, 2 SVD, 3 U pass, 4 V step, 5 rotation
-  std::vector<int> ev_kind;
-  size_t ev_used = 0;
+  std::vector<int> ev_kind[2];
+  size_t ev_used[2] = {0, 0};
+  int cur = 0;
   double t_kind[6] = {0, 0, 0, 0, 0, 0};
 
   ~Solver() {
-    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    for (auto& pool : ev)
+      for (cudaEvent_t e : pool) cudaEventDestroy(e);
   }
 
   int ev_begin(int kind) {
     if (!profile) return BGPU_OK;
-    if (ev_used + 2 > ev.size()) {
+    auto& pool = ev[cur];
+    size_t& used = ev_used[cur];
+    if (used + 2 > pool.size()) {
       for (int i = 0; i < 2; ++i) {
         cudaEvent_t e;
         BGPU_CUDA(cudaEventCreate(&e));
-        ev.push_back(e);
+        pool.push_back(e);
       }
-      ev_kind.push_back(0);
+      ev_kind[cur].push_back(0);
     }
-    ev_kind[ev_used / 2] = kind;
-    BGPU_CUDA(cudaEventRecord(ev[ev_used], s));
+    ev_kind[cur][used / 2] = kind;
+    BGPU_CUDA(cudaEventRecord(pool[used], s));
     return BGPU_OK;
   }
   int ev_end() {
     if (!profile) return BGPU_OK;
-    BGPU_CUDA(cudaEventRecord(ev[ev_used + 1], s));
-    ev_used += 2;
+    BGPU_CUDA(cudaEventRecord(ev[cur][ev_used[cur] + 1], s));
+    ev_used[cur] += 2;
     return BGPU_OK;
   }
-  // Called after the stream has been synchronised.
-  int ev_collect() {
-    for (size_t i = 0; i < ev_used; i += 2) {
+  // Reads a pool whose events have all completed (the stream was
+  // synchronised after the last of them).
+  int ev_collect(int pool) {
+    for (size_t i = 0; i < ev_used[pool]; i += 2) {
       float ms = 0.f;
-      BGPU_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
-      t_kind[ev_kind[i / 2]] += ms * 1e-3;
+      BGPU_CUDA(cudaEventElapsedTime(&ms, ev[pool][i], ev[pool][i + 1]));
+      t_kind[ev_kind[pool][i / 2]] += ms * 1e-3;
     }
-    ev_used = 0;
+    ev_used[pool] = 0;
     return BGPU_OK;
   }
 
@@ -437,7 +444,8 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
                               cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaMemcpyAsync(&derr, S.derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaStreamSynchronize(s));
-    BGPU_TRY(S.ev_collect());
+    const int done_pool = S.cur;  // this restart's events, read after the rotation
+    S.cur ^= 1;
     {
       BGPU_REQUIRE(derr == 0, BGPU_ERR_DEVICE,
                    "a bulk copy into shared memory did not complete within its "
@@ -477,6 +485,7 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     BGPU_CUDA(cudaMemcpyAsync(S.Vnew.as<float>() + (uint64_t)kc * S.ldv,
                               S.rem.p, g * 4, cudaMemcpyDeviceToDevice, s));
     BGPU_TRY(S.ev_end());
+    BGPU_TRY(S.ev_collect(done_pool));  // the rotation runs meanwhile
     std::swap(S.U.p, S.Unew.p);
     std::swap(S.V.p, S.Vnew.p);
     S.launches += 2;
@@ -505,6 +514,8 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
                               cudaMemcpyDeviceToHost, s));
   }
   BGPU_CUDA(cudaStreamSynchronize(s));
+  BGPU_TRY(S.ev_collect(0));  // whatever the last restarts left in the pools
+  BGPU_TRY(S.ev_collect(1));
   if (info) {
     info->converged = converged ? 1 : 0;
     info->restarts = restarts;

@@ -310,18 +310,31 @@ def _subset(X, qc, hvg):
     return X
 
 
+def _full_loadings(ld, hvg, num_all_genes: int):
+    """Loadings over every gene (the varm layout): NaN rows for genes outside
+    the HVG mask."""
+    if hvg is None:
+        return ld
+    full = np.full((num_all_genes, ld.shape[1]), np.nan, dtype=np.float32)
+    full[hvg] = ld
+    return full
+
+
 def pca(X, *others, QC_column=None, hvg_column=None, num_PCs: int = 50,
         subspace_size: int = 100, tolerance: float = 1e-6,
         max_iterations: int = 100, chunk_size: int = 1024, seed: int = 0,
         match_parallel: bool = False, verbose: bool = False,
-        num_threads=None, return_result: bool = False):
+        num_threads=None, loadings: bool = False, return_result: bool = False):
     """``SingleCell.pca()`` for scipy sparse matrices of normalised counts.
 
     ``X`` (and each of ``others``) is a float32 cells x genes CSR/CSC matrix,
     as ``SingleCell.normalize()`` leaves it. ``QC_column`` / ``hvg_column``
     are Boolean masks (or sequences of masks, one per dataset, or None).
     Returns the PCs array (cells x num_PCs, float32, NaN rows for cells that
-    failed QC), or a tuple of arrays when ``others`` are given.
+    failed QC), or a tuple of arrays when ``others`` are given. With
+    ``loadings=True`` returns ``(PCs, loadings)``: the right singular vectors,
+    genes x num_PCs float32 over every gene of ``X`` (a varm-shaped array),
+    NaN for genes outside ``hvg_column``; one array shared by all datasets.
     """
     import scipy.sparse as sp
     datasets = [X, *others]
@@ -367,7 +380,7 @@ def pca(X, *others, QC_column=None, hvg_column=None, num_PCs: int = 50,
     M = DeviceMatrix(Xall.indptr, Xall.indices, Xall.data, num_cells, num_genes)
     try:
         res = M.solve(num_PCs, subspace_size, tolerance, max_iterations, seed,
-                      chunk_size)
+                      chunk_size, loadings=loadings)
     finally:
         M.close()
     if not res.converged and verbose:
@@ -384,6 +397,8 @@ def pca(X, *others, QC_column=None, hvg_column=None, num_PCs: int = 50,
             part = full
         outs.append(part)
     out = outs[0] if nd == 1 else tuple(outs)
+    if loadings:
+        out = (out, _full_loadings(res.loadings, hvgs[0], datasets[0].shape[1]))
     return (out, res) if return_result else out
 
 
@@ -399,7 +414,8 @@ def pca_counts(counts, *, method: str = "logCP10k", QC_column=None,
     on the GPU over all genes (as ``normalize()`` does, brisc/normalize.pyx:
     36-81, with the QC mask for log1pPF's mean), then the QC cells and HVG
     genes are selected and PCA runs on log1p(count * factor) without ever
-    storing the normalised values.
+    storing the normalised values. ``loadings=True`` returns ``(PCs,
+    loadings)`` as :func:`pca` does.
     """
     import scipy.sparse as sp
     import torch
@@ -437,6 +453,8 @@ def pca_counts(counts, *, method: str = "logCP10k", QC_column=None,
         full = np.full((n, num_PCs), np.nan, dtype=np.float32)
         full[qc] = out
         out = full
+    if loadings:
+        out = (out, _full_loadings(res.loadings, hvg, G))
     return (out, res) if return_result else out
 
 

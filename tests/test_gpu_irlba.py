@@ -164,6 +164,23 @@ def test_pca_qc_backfill_and_joint(cuda, golden):
     assert np.array_equal(np.vstack([a, b]), joint)
 
 
+def test_pca_loadings_in_varm_layout(cuda, golden):
+    """pca(..., loadings=True): loadings over every gene (NaN outside the HVG
+    mask); on the HVGs they are the right singular vectors (A^T u = s v)."""
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, "clustered_a")
+    hvg = (np.arange(g) % 7) != 3
+    (pcs, ld), res = bg.pca(X, hvg_column=hvg, num_PCs=k, subspace_size=m,
+                            loadings=True, return_result=True)
+    assert ld.shape == (g, k) and ld.dtype == np.float32
+    assert np.isnan(ld[~hvg]).all() and np.isfinite(ld[hvg]).all()
+    Xh = sp.csr_matrix(X[:, np.flatnonzero(hvg)])
+    S, U, Vt = dense.top_svd(Xh, k + 2)
+    j = max(dense.gap_mask(S, k, 0.01))
+    assert dense.max_angle(ld[hvg][:, :j], Vt.T[:, :j]) < 1e-3
+    np.testing.assert_allclose(np.linalg.norm(ld[hvg], axis=0), 1.0, rtol=1e-4)
+
+
 def test_nonconverged_returns_ritz_vectors(cuda, golden):
     z = golden("irlba")
     X, n, g, k, m = _case(z, "clustered_a")
