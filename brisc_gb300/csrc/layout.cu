@@ -683,7 +683,7 @@ void matrix_free(Matrix* m) {
   void* ptrs[] = {m->rowptr, m->csr_packed, m->csr_val, m->csr_col,
                   m->colptr, m->csc_packed, m->csc_val, m->csc_row,
                   m->isf,    m->post,       m->sd,      m->rtab_r,
-                  m->rtab_c, m->csc16};
+                  m->rtab_c, m->csc16,      m->row_order};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   *m = Matrix();

@@ -65,6 +65,7 @@ struct Matrix {
   float* rtab_r = nullptr;  // [cell][kCountTab] (X.v)
   float* rtab_c = nullptr;  // [panel][kCountTab][P] (X^T.u)
   uint16_t* csc16 = nullptr;  // compact panel entries (stream16.cu)
+  int32_t* row_order = nullptr;  // X.v row schedule, longest rows first
 
   float* sd = nullptr;  // cached clipped gene std (computed on first use)
   int device = 0;

@@ -25,6 +25,7 @@
 // result depends only on the data and the layout, not on timing or launch
 // shape, so repeated products are bit-identical.
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <vector>
 
@@ -83,8 +84,8 @@ __device__ __noinline__ float csr_row_exact8(const uint32_t* __restrict__ packed
 constexpr int kTabSlot = 17;  // padded per-group table slot (conflict-free)
 
 __global__ void __launch_bounds__(256, 4)
-k_spmv_rows(CsrView X, const float* __restrict__ v, const float* __restrict__ sd,
-            float* __restrict__ y) {
+k_spmv_rows(CsrView X, const int32_t* __restrict__ order, const float* __restrict__ v,
+            const float* __restrict__ sd, float* __restrict__ y) {
   extern __shared__ __align__(16) float sm[];
   float* w = sm;                                       // g floats
   float* tabs = sm + ((X.g + 3) & ~3u);                // 32 groups x 2 x kTabSlot
@@ -101,16 +102,23 @@ k_spmv_rows(CsrView X, const float* __restrict__ v, const float* __restrict__ sd
   const uint64_t ngroups = (gridDim.x * (uint64_t)blockDim.x) >> 3;
   const float2* rt2 = reinterpret_cast<const float2*>(X.rtab);
 
+  // Rows are taken in `order` (longest first, by 32-entry windows), so the
+  // four groups of a warp work on rows of about the same length; each row's
+  // sum is the same whichever group computes it.
+  auto row_at = [&](uint64_t i) -> uint64_t { return order ? (uint64_t)order[i] : i; };
   // offsets and count table of the next row, loaded one row ahead
   int64_t nx0 = 0, nx1 = 0;
   float2 nt2 = make_float2(0.f, 0.f);
+  uint64_t nrow = 0;
   if (gid < X.n) {
-    nx0 = X.rowptr[gid];
-    nx1 = X.rowptr[gid + 1];
-    nt2 = rt2[gid * (kCountTab / 2) + lane8];
+    nrow = row_at(gid);
+    nx0 = X.rowptr[nrow];
+    nx1 = X.rowptr[nrow + 1];
+    nt2 = rt2[nrow * (kCountTab / 2) + lane8];
   }
   int buf = 0;
-  for (uint64_t r = gid; r < X.n; r += ngroups, buf ^= 1) {
+  for (uint64_t i = gid; i < X.n; i += ngroups, buf ^= 1) {
+    const uint64_t r = nrow;
     const int64_t e0 = nx0, e1 = nx1;
     const float2 t2 = nt2;
     // row-relative 32-bit offsets: the row's words are [lead, len) of the
@@ -125,11 +133,11 @@ k_spmv_rows(CsrView X, const float* __restrict__ v, const float* __restrict__ sd
     const uint4 q1 = o + 32 < len ? ld_stream_u4(rowp + o + 32) : z4;
     const uint4 q2 = o + 64 < len ? ld_stream_u4(rowp + o + 64) : z4;
     const uint4 q3 = o + 96 < len ? ld_stream_u4(rowp + o + 96) : z4;
-    const uint64_t rn = r + ngroups;
-    if (rn < X.n) {
-      nx0 = X.rowptr[rn];
-      nx1 = X.rowptr[rn + 1];
-      nt2 = rt2[rn * (kCountTab / 2) + lane8];
+    if (i + ngroups < X.n) {
+      nrow = row_at(i + ngroups);
+      nx0 = X.rowptr[nrow];
+      nx1 = X.rowptr[nrow + 1];
+      nt2 = rt2[nrow * (kCountTab / 2) + lane8];
     }
     // the row's count table into this group's (double-buffered) slot
     float* tb = tabs + gslot + buf * kTabSlot;
@@ -633,6 +641,34 @@ __global__ void k_count_tables(const float* __restrict__ isf, uint64_t n,
 
 }  // namespace
 
+// Row order for X.v (matrix creation): rows by descending count of 32-entry
+// windows (the 8-lane groups' passes), stable, by a counting sort on the host.
+// BGPU_ROW_ORDER=0 keeps the natural order (A/B study).
+int build_row_order(Matrix* m, cudaStream_t s, uint64_t* bytes_acc) {
+  const char* e = std::getenv("BGPU_ROW_ORDER");
+  if ((e && e[0] == '0') || m->n < 2 || m->n >= (uint64_t)INT32_MAX) return BGPU_OK;
+  std::vector<int64_t> rp(m->n + 1);
+  BGPU_CUDA(cudaMemcpyAsync(rp.data(), m->rowptr, (m->n + 1) * 8, cudaMemcpyDeviceToHost, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));
+  constexpr uint64_t kCap = 4096;  // rows of >= 4096 windows share the top bucket
+  std::vector<uint32_t> key(m->n);
+  std::vector<uint64_t> cnt(kCap + 1, 0);
+  for (uint64_t r = 0; r < m->n; ++r) {
+    const uint64_t w = std::min<uint64_t>(kCap, (uint64_t)(rp[r + 1] - rp[r] + 31) / 32);
+    key[r] = (uint32_t)(kCap - w);  // descending windows
+    ++cnt[key[r]];
+  }
+  uint64_t run = 0;
+  for (auto& c : cnt) { const uint64_t t = c; c = run; run += t; }
+  std::vector<int32_t> order(m->n);
+  for (uint64_t r = 0; r < m->n; ++r) order[cnt[key[r]]++] = (int32_t)r;
+  BGPU_CUDA(cudaMallocAsync((void**)&m->row_order, m->n * 4, s));
+  *bytes_acc += m->n * 4;
+  BGPU_CUDA(cudaMemcpyAsync(m->row_order, order.data(), m->n * 4, cudaMemcpyHostToDevice, s));
+  BGPU_CUDA(cudaStreamSynchronize(s));  // `order` is a host temporary
+  return BGPU_OK;
+}
+
 bool stream_supported(const Matrix& m) {
   return m.mode == kCounts && m.P <= (uint32_t)kMaxPanelRows &&
          SegLayout(m.P, m.g).total <= 220 * 1024;
@@ -661,6 +697,7 @@ int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
                                                                     m->csr_packed);
     BGPU_CHECK_LAUNCH();
   }
+  BGPU_TRY(build_row_order(m, s, bytes_acc));
   m->stream_ok = true;
   // BGPU_COMPACT=0 keeps X^T.u on the 32-bit panel words (A/B study)
   const char* ec = std::getenv("BGPU_COMPACT");
@@ -687,7 +724,7 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
   const uint64_t want = ceil_div(m.n, 32);
   const unsigned grid = (unsigned)std::max<uint64_t>(
       1, std::min<uint64_t>(want, (uint64_t)num_sms() * 4));
-  k_spmv_rows<<<grid, 256, smem, s>>>(X, v, sd, y);
+  k_spmv_rows<<<grid, 256, smem, s>>>(X, m.row_order, v, sd, y);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
