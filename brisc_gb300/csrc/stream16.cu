@@ -31,14 +31,17 @@ constexpr int kR16Threads = 384;
 constexpr int kR16Warps = kR16Threads / 32;
 constexpr int kR16Rows = 1024;  // panel rows the 10-bit row field allows
 
+constexpr int kStageLd = 33;  // per-warp [position][lane] staging, padded
+
 struct Seg16Layout {
-  uint32_t tab, cps, nz, misc, total;
+  uint32_t tab, cps, nz, misc, stage, total;
   __host__ __device__ Seg16Layout(uint32_t P, uint32_t g) {
     tab = 128;                              // mbarrier
     cps = tab + r128b(P * kTab16 * 4);      // table scaled by u: [count][row]
     nz = cps + r128b((g + 1) * 4);          // gene offsets, then per-gene sums
     misc = nz + r128b(g * 2);               // non-empty genes in order (u16)
-    total = misc + 128;                     // warp totals
+    stage = misc + 128;                     // warp totals (above), then the
+    total = stage + r128b(kR16Warps * 15 * kStageLd * 4);  // lanes' running sums
   }
 };
 
@@ -147,6 +150,7 @@ k_rmat_seg16(CscView X, const uint16_t* __restrict__ e16, const float* __restric
   const int64_t beg = pbase + s0, end = pbase + s1;
   const uint32_t pshift = X.pshift;
   const uint32_t lt = lanemask_lt16();
+  float* stg = reinterpret_cast<float*>(smem + L.stage) + wid * 15 * kStageLd + lane;
   float carry = 0.f;
   uint32_t kb = 0;
   const uint4 z4 = make_uint4(0, 0, 0, 0);
@@ -220,18 +224,26 @@ k_rmat_seg16(CscView X, const uint16_t* __restrict__ e16, const float* __restric
       if (lane >= d) hs += t;
     }
     const uint32_t kl = kb + hs - h;
-    // a head closes the segment before it (the run's first head closes nothing)
+    // a head closes the segment before it (the run's first head closes
+    // nothing); each lane walks only its own heads, reading the running sum
+    // before the head from its staging column
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      if ((hm >> i) & 1u) {
-        const uint32_t pre = hm & ((1u << i) - 1u);
-        const uint32_t k = kl + __popc(pre);
-        if (k > 0) {
-          const float val = i == 0 ? cin : (pre ? sl[i - 1] : cin + sl[i - 1]);
-          gsum[nz[i0 + k - 1]] = val;
+    for (int i = 0; i < 15; ++i) stg[i * kStageLd] = sl[i];
+    __syncwarp();
+    for (uint32_t rem = hm; rem != 0u; rem &= rem - 1u) {
+      const int i = __ffs(rem) - 1;
+      const uint32_t pre = hm & ((1u << i) - 1u);
+      const uint32_t k = kl + __popc(pre);
+      if (k > 0) {
+        float val = cin;
+        if (i > 0) {
+          const float sv = stg[(i - 1) * kStageLd];
+          val = pre ? sv : cin + sv;
         }
+        gsum[nz[i0 + k - 1]] = val;
       }
     }
+    __syncwarp();
     carry = __shfl_sync(0xffffffffu, T, 31);
     kb += __shfl_sync(0xffffffffu, hs, 31);
   }
