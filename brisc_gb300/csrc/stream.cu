@@ -184,14 +184,24 @@ constexpr int kSegThreads = 512;
 constexpr int kMaxPanelRows = 2048;  // rows per panel the staged table allows
 constexpr int kSegWarps = kSegThreads / 32;
 
+constexpr int kRmatThreads = 384;
+constexpr int kRmatWarps = kRmatThreads / 32;
+constexpr int kStageLd = 33;  // per-warp [position][lane] staging, padded
+
+// Bytes of one block's staged running sums: 7 positions x 32 lanes per warp.
+__host__ __device__ constexpr uint32_t stage_bytes(int warps) {
+  return (uint32_t)warps * 7u * kStageLd * 4u;
+}
+
 struct SegLayout {
-  uint32_t tab, cps, nz, misc, total;
+  uint32_t tab, cps, nz, misc, stage, total;
   __host__ __device__ SegLayout(uint32_t P, uint32_t g) {
     tab = 128;                             // mbarrier
     cps = tab + r128(P * kCountTab * 4);   // table scaled by u: [count][row]
     nz = cps + r128((g + 1) * 4);          // gene offsets, then per-gene sums
     misc = nz + r128(g * 2);               // non-empty genes in order (u16)
-    total = misc + 128;                    // warp totals
+    stage = misc + 128;                    // warp totals (above), then the
+    total = stage + r128(stage_bytes(kRmatWarps));  // lanes' running sums
   }
 };
 
@@ -208,9 +218,6 @@ __device__ __forceinline__ float scaled_u(const CscView& X, const float* u,
   const float uu = u_scale ? u[r] * scale : u[r];
   return X.post ? uu * X.post[r] : uu;
 }
-
-constexpr int kRmatThreads = 384;
-constexpr int kRmatWarps = kRmatThreads / 32;
 
 __global__ void __launch_bounds__(kRmatThreads, 2)
 k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_scale,
@@ -306,6 +313,7 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
   const int64_t beg = pbase + s0, end = pbase + s1;
   const uint32_t pshift = X.pshift, lrmask = P - 1;
   const uint32_t lt = lanemask_lt();
+  float* stg = reinterpret_cast<float*>(smem + L.stage) + wid * 7 * kStageLd + lane;
   float carry = 0.f;  // open segment's sum entering the next iteration
   uint32_t kb = 0;    // heads seen in earlier iterations
   // software-pipelined: the next iteration's 32 bytes per lane are in flight
@@ -382,16 +390,22 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
       if (lane >= d) hs += t;
     }
     const uint32_t kl = kb + hs - h;  // heads before this lane
-    // a head closes the segment before it (the run's first head closes nothing)
+    // a head closes the segment before it (the run's first head closes
+    // nothing); each lane walks only its own heads, reading the running sum
+    // before the head from its staging column
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if ((hm >> i) & 1u) {
-        const uint32_t pre = hm & ((1u << i) - 1u);
-        const uint32_t k = kl + __popc(pre);
-        if (k > 0) {
-          const float val = i == 0 ? cin : (pre ? sl[i - 1] : cin + sl[i - 1]);
-          gsum[nz[i0 + k - 1]] = val;
+    for (int i = 0; i < 7; ++i) stg[i * kStageLd] = sl[i];
+    for (uint32_t rem = hm; rem != 0u; rem &= rem - 1u) {
+      const int i = __ffs(rem) - 1;
+      const uint32_t pre = hm & ((1u << i) - 1u);
+      const uint32_t k = kl + __popc(pre);
+      if (k > 0) {
+        float val = cin;
+        if (i > 0) {
+          const float sv = stg[(i - 1) * kStageLd];
+          val = pre ? sv : cin + sv;
         }
+        gsum[nz[i0 + k - 1]] = val;
       }
     }
     carry = __shfl_sync(0xffffffffu, T, 31);
@@ -410,7 +424,7 @@ k_rmat_seg(CscView X, const float* __restrict__ u, const float* __restrict__ u_s
 // shared with X^T.u) arrives by bulk copy; each lane tracks the row of its
 // words from the head flags.
 struct RowSegLayout {
-  uint32_t tab, w, rofs, nzr, rsum, misc, total;
+  uint32_t tab, w, rofs, nzr, rsum, misc, stage, total;
   __host__ __device__ RowSegLayout(uint32_t P, uint32_t g) {
     tab = 128;                             // mbarrier
     w = tab + r128(P * kCountTab * 4);     // count table [count][row]
@@ -418,7 +432,8 @@ struct RowSegLayout {
     nzr = rofs + r128((P + 1) * 4);        // row offsets in the panel
     rsum = nzr + r128(P * 2);              // non-empty rows in order (u16)
     misc = rsum + r128(P * 4);             // per-row sums
-    total = misc + 128;                    // warp totals
+    stage = misc + 128;                    // warp totals (above), then the
+    total = stage + r128(stage_bytes(kSegWarps));  // lanes' running sums
   }
 };
 
@@ -493,6 +508,7 @@ k_spmv_seg(CsrView X, uint32_t pshift, const float* __restrict__ rtab_c,
 
   const int64_t beg = pbase + s0, end = pbase + s1;
   const uint32_t lt = lanemask_lt();
+  float* stg = reinterpret_cast<float*>(smem + L.stage) + wid * 7 * kStageLd + lane;
   float carry = 0.f;
   uint32_t kb = 0;
   for (int64_t b = beg & ~7ll; b < end; b += 256) {
@@ -565,14 +581,18 @@ k_spmv_seg(CsrView X, uint32_t pshift, const float* __restrict__ rtab_c,
     float cin = __shfl_up_sync(0xffffffffu, T, 1);
     if (lane == 0) cin = carry;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if ((hm >> i) & 1u) {
-        const uint32_t pre = hm & ((1u << i) - 1u);
-        const uint32_t k = kl + __popc(pre);
-        if (k > 0) {
-          const float val = i == 0 ? cin : (pre ? sl[i - 1] : cin + sl[i - 1]);
-          rsum[nzr[i0 + k - 1]] = val;
+    for (int i = 0; i < 7; ++i) stg[i * kStageLd] = sl[i];
+    for (uint32_t rem = hm; rem != 0u; rem &= rem - 1u) {
+      const int i = __ffs(rem) - 1;
+      const uint32_t pre = hm & ((1u << i) - 1u);
+      const uint32_t k = kl + __popc(pre);
+      if (k > 0) {
+        float val = cin;
+        if (i > 0) {
+          const float sv = stg[(i - 1) * kStageLd];
+          val = pre ? sv : cin + sv;
         }
+        rsum[nzr[i0 + k - 1]] = val;
       }
     }
     carry = __shfl_sync(0xffffffffu, T, 31);
