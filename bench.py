@@ -62,7 +62,9 @@ def parse():
     ap.add_argument("--cells", type=int, default=0, help="override cell count")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--reorth-passes", type=int, default=2)
+    ap.add_argument("--reorth-passes", default="auto",
+                    type=lambda x: x if x == "auto" else int(x),
+                    help="U-side Gram-Schmidt passes: auto (adaptive), 1 or 2")
     ap.add_argument("--sample-rows", type=int, default=125_000)
     ap.add_argument("--concurrency", type=int, default=16,
                     help="concurrent solves (batched_3m, serve)")
@@ -384,6 +386,7 @@ def run_ours(args):
            "gpu_launches": int(launch_total),
            "solve": {"restarts": last.info["restarts"],
                      "lanczos_steps": last.info["lanczos_steps"],
+                     "second_passes": last.info["second_passes"],
                      "converged": last.converged,
                      "seconds_host": last.info["seconds"]}}
     print(json.dumps(out))

@@ -74,6 +74,7 @@ class SolveInfo(C.Structure):
         ("reorth_bytes", C.c_double),
         ("rotation_bytes", C.c_double),
         ("kernel_launches", C.c_uint64),
+        ("second_passes", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

@@ -98,7 +98,7 @@ class _U16View:
 def pca_subsets(shared: SharedMatrix, subsets, *, num_PCs: int = 30,
                 subspace_size: int | None = None, tolerance: float = 1e-6,
                 max_iterations: int = 100, seed: int = 0, concurrency: int = 8,
-                reorth_passes: int = 2) -> list[SubsetResult]:
+                reorth_passes: int | str = "auto") -> list[SubsetResult]:
     """One IRLBA PCA per row subset of `shared`, `concurrency` at a time.
 
     `subsets` is a sequence of int64 row-index arrays. Returns one

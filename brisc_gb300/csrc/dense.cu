@@ -22,10 +22,20 @@ __device__ __forceinline__ float dot4(float4 a, float4 b) {
   return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
 }
 
+// Adaptive second Gram-Schmidt pass: gate = {|y1|^2, |y0 - mean|^2} of the
+// first pass. When the first pass kept at least half of the squared norm, y1
+// is orthogonal to U to working precision (Kahan-Parlett "twice is enough")
+// and the second pass's kernels return at once. Every block of every kernel
+// reads the same two numbers and takes the same decision.
+__device__ __forceinline__ bool second_pass_skipped(const float* gate) {
+  return gate != nullptr && gate[0] >= 0.5f * gate[1];
+}
+
 __global__ void __launch_bounds__(256)
 k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
         const float* __restrict__ y, float* __restrict__ part,
-        uint32_t pstride, int with_sum) {
+        uint32_t pstride, int with_sum, const float* __restrict__ gate) {
+  if (second_pass_skipped(gate)) return;
   __shared__ float red[8][9];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint64_t b = blockIdx.x;
@@ -73,18 +83,31 @@ k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
 __global__ void __launch_bounds__(256)
 k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
           const float* __restrict__ coef, const float* __restrict__ mean_sum,
-          uint64_t n, const float* __restrict__ y_in, float* __restrict__ y_out,
-          float* __restrict__ norm_part, uint32_t pstride) {
+          uint64_t n, const float* y_in, float* y_out,  // may be the same
+          float* __restrict__ norm_part, uint32_t pstride, int with_centred,
+          const float* __restrict__ gate, unsigned long long* __restrict__ taken) {
+  if (second_pass_skipped(gate)) return;
+  if (taken && blockIdx.x == 0 && threadIdx.x == 0) {
+    taken[0] += 1ull;
+    taken[1] += ncols;
+  }
   extern __shared__ float cs[];
-  __shared__ float red[8];
+  __shared__ float red[2][8];
   for (uint32_t c = threadIdx.x; c < ncols; c += blockDim.x) cs[c] = coef[c];
   __syncthreads();
   const uint64_t b = blockIdx.x;
   const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
-  float sq = 0.f;
+  float sq = 0.f, sqc = 0.f;
   if (row0 < ldu) {
     float4 yv = *reinterpret_cast<const float4*>(y_in + row0);
     const float mean = mean_sum ? (*mean_sum) / (float)n : 0.f;  // pca.pyx:1025-1028
+    if (with_centred) {  // |y_in - mean|^2 over the block's rows < n
+      const float cx = (row0 + 0 < n) ? yv.x - mean : 0.f;
+      const float cy = (row0 + 1 < n) ? yv.y - mean : 0.f;
+      const float cz = (row0 + 2 < n) ? yv.z - mean : 0.f;
+      const float cw = (row0 + 3 < n) ? yv.w - mean : 0.f;
+      sqc = cx * cx + cy * cy + cz * cz + cw * cw;
+    }
     float4 t = make_float4(mean, mean, mean, mean);
 #pragma unroll 8
     for (uint32_t c = 0; c < ncols; ++c) {
@@ -104,12 +127,16 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   }
   if (norm_part) {
     sq = warp_sum(sq);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sq;
+    if (with_centred) sqc = warp_sum(sqc);
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = sq;
+      red[1][threadIdx.x >> 5] = sqc;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < (with_centred ? 2u : 1u)) {
       float t = 0.f;
-      for (int w = 0; w < 8; ++w) t += red[w];
-      norm_part[b * pstride] = t;
+      for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
+      norm_part[b * pstride + threadIdx.x] = t;
     }
   }
 }
@@ -177,13 +204,24 @@ k_uupdate_dots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
 // order, a fixed order whatever the timing.
 __global__ void __launch_bounds__(1024)
 k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
-              uint32_t ncols, float* __restrict__ out) {
+              uint32_t ncols, float* __restrict__ out, const float* __restrict__ gate) {
+  if (second_pass_skipped(gate)) return;
   __shared__ float ws[32][33];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t c = blockIdx.x * 32 + lane;
   float t = 0.f;
-  if (c < ncols)
-    for (uint64_t b = wid; b < nblocks; b += 32) t += part[b * pstride + c];
+  if (c < ncols) {
+    // eight loads in flight, added in block order
+    uint64_t b = wid;
+    for (; b + 32 * 7 < nblocks; b += 32 * 8) {
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = part[(b + 32 * i) * pstride + c];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) t += v[i];
+    }
+    for (; b < nblocks; b += 32) t += part[b * pstride + c];
+  }
   ws[wid][lane] = t;
   __syncthreads();
   if (wid == 0 && c < ncols) {
@@ -281,12 +319,18 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) float vsm[];
   const uint32_t slice = (g + kVCluster - 1) / kVCluster;
+  // passes == 0: adaptive, a second pass only where the first kept less than
+  // half of the squared norm of z - alpha v_j (all CTAs take one decision)
+  const bool adaptive = passes == 0;
+  const int npass = adaptive ? 2 : passes;
   float* zs = vsm;                            // slice
-  float* pd = zs + ((slice + 3) & ~3u);       // 2 x m partial dots (per pass)
-  float* dots = pd + 2 * m;                   // m
-  float* upd = dots + ((m + 3) & ~3u);        // kVSplit x slice partial updates
+  float* pd = zs + ((slice + 3) & ~3u);       // 2 x (m + 1) partials (per pass)
+  float* dots = pd + 2 * (m + 1);             // m + 1
+  float* upd = dots + ((m + 4) & ~3u);        // kVSplit x slice partial updates
   __shared__ double pn;                       // partial squared norm
   __shared__ double wred[kVThreads / 32];
+  __shared__ float wz[kVThreads / 32];
+  __shared__ float pz1;                       // partial |z after pass 0|^2
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t q = cluster.block_rank();
   const uint32_t c0 = q * slice, c1 = min(g, c0 + slice);
@@ -295,17 +339,23 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
   for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
     zs[c - c0] = zin[c] - alpha * vj[c];  // pca.pyx:1104-1105
   __syncthreads();
-  for (int pass = 0; pass < passes; ++pass) {
-    float* pdp = pd + (pass & 1) * m;
-    for (uint32_t col = wid; col <= j; col += kVThreads / 32) {
-      const float* vc = V + (uint64_t)col * ldv;
+  for (int pass = 0; pass < npass; ++pass) {
+    float* pdp = pd + (pass & 1) * (m + 1);
+    // adaptive: pass 0 also sums |z|^2 as column j + 1
+    const uint32_t ncol = j + 1 + (adaptive && pass == 0 ? 1u : 0u);
+    for (uint32_t col = wid; col < ncol; col += kVThreads / 32) {
       float d = 0.f;
-      for (uint32_t c = c0 + lane; c < c1; c += 32) d += vc[c] * zs[c - c0];
+      if (col <= j) {
+        const float* vc = V + (uint64_t)col * ldv;
+        for (uint32_t c = c0 + lane; c < c1; c += 32) d += vc[c] * zs[c - c0];
+      } else {
+        for (uint32_t c = c0 + lane; c < c1; c += 32) d += zs[c - c0] * zs[c - c0];
+      }
       d = warp_sum(d);
       if (lane == 0) pdp[col] = d;
     }
     cluster.sync();  // every CTA's partials are visible
-    for (uint32_t col = threadIdx.x; col <= j; col += kVThreads) {
+    for (uint32_t col = threadIdx.x; col < ncol; col += kVThreads) {
       float t = 0.f;
       for (uint32_t r = 0; r < kVCluster; ++r) t += cluster.map_shared_rank(pdp, r)[col];
       dots[col] = t;
@@ -330,6 +380,23 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
       zs[i] -= t;
     }
     __syncthreads();
+    if (adaptive && pass == 0) {
+      float s1 = 0.f;
+      for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
+        s1 += zs[c - c0] * zs[c - c0];
+      s1 = warp_sum(s1);
+      if (lane == 0) wz[wid] = s1;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < kVThreads / 32; ++w) t += wz[w];
+        pz1 = t;
+      }
+      cluster.sync();
+      float z1 = 0.f;
+      for (uint32_t r = 0; r < kVCluster; ++r) z1 += *cluster.map_shared_rank(&pz1, r);
+      if (z1 >= 0.5f * dots[j + 1]) break;  // the same in every CTA
+    }
   }
   float* out = (j + 1 < m) ? V + (uint64_t)(j + 1) * ldv : rem;
   if (j + 1 < m) {
@@ -454,9 +521,9 @@ __global__ void k_b_to_float(const double* __restrict__ B, uint64_t count,
 
 int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
                  uint64_t nblocks, float* part, uint32_t pstride, bool with_sum,
-                 cudaStream_t s) {
+                 cudaStream_t s, const float* gate) {
   k_udots<<<(unsigned)nblocks, 256, 0, s>>>(U, ldu, ncols, y, part, pstride,
-                                            with_sum ? 1 : 0);
+                                            with_sum ? 1 : 0, gate);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -464,9 +531,12 @@ int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
 int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    const float* coef, const float* mean_sum, uint64_t n,
                    const float* y_in, float* y_out, uint64_t nblocks,
-                   float* norm_part, uint32_t pstride, cudaStream_t s) {
+                   float* norm_part, uint32_t pstride, cudaStream_t s,
+                   bool with_centred, const float* gate,
+                   unsigned long long* taken) {
   k_uupdate<<<(unsigned)nblocks, 256, std::max<size_t>(ncols, 1) * 4, s>>>(
-      U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride);
+      U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride,
+      with_centred ? 1 : 0, gate, taken);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -492,10 +562,12 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
 }
 
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
-                       uint32_t ncols, float* out, cudaStream_t s) {
+                       uint32_t ncols, float* out, cudaStream_t s,
+                       const float* gate) {
   if (ncols == 0) return BGPU_OK;
   k_reduce_cols<<<(unsigned)ceil_div(ncols, 32), 1024, 0, s>>>(part, nblocks,
-                                                               pstride, ncols, out);
+                                                               pstride, ncols, out,
+                                                               gate);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -512,14 +584,14 @@ int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
                  uint32_t j, uint32_t m, const float* scal, double* B,
                  float* rem, int passes, cudaStream_t s) {
   const uint32_t slice = (g + kVCluster - 1) / kVCluster;
-  const size_t csm = ((size_t)((slice + 3) & ~3u) + 2ull * m + ((m + 3) & ~3u) +
-                      (size_t)kVSplit * slice) * sizeof(float);
+  const size_t csm = ((size_t)((slice + 3) & ~3u) + 2ull * (m + 1) +
+                      ((m + 4) & ~3u) + (size_t)kVSplit * slice) * sizeof(float);
   if (csm <= 48 * 1024) {
     k_vstep_cluster<<<kVCluster, kVThreads, csm, s>>>(z, V, ldv, g, j, m, scal, B,
                                                      rem, passes);
   } else {
-    k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(
-        z, V, ldv, g, j, m, scal, B, rem, passes);
+    k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(  // adaptive: 2 passes
+        z, V, ldv, g, j, m, scal, B, rem, passes == 0 ? 2 : passes);
   }
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;

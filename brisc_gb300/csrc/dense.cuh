@@ -9,18 +9,28 @@ constexpr int kRowBlock = 1024;  // rows per fixed reduction block (256 threads 
 
 // part[b * pstride + c] = U[rows of b, c] . y[rows of b]   for c < ncols
 // and, when with_sum, part[b * pstride + ncols] = sum(y[rows of b]).
+//
+// Adaptive second pass: the dots, reduce and update kernels take an optional
+// device `gate` = {|y1|^2, |y0 - mean|^2} of the first pass and return at
+// once, writing nothing, when gate[0] >= gate[1] / 2 (the first pass kept at
+// least half of the squared norm: "twice is enough", Kahan-Parlett).
 int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
                  uint64_t nblocks, float* part, uint32_t pstride, bool with_sum,
-                 cudaStream_t s);
+                 cudaStream_t s, const float* gate = nullptr);
 
 // y_out = y_in - (mean + U[:, :ncols] . coef)   for rows < n, 0 beyond.
 // mean = (*mean_sum) / n when mean_sum is non-null (the reference's
 // `dot_product = mean; dot_product += U[row, col] * work[col]`, pca.pyx:1045).
-// When norm_part is non-null, norm_part[b * pstride] = sum(y_out^2) per block.
+// When norm_part is non-null, norm_part[b * pstride] = sum(y_out^2) per block,
+// and with with_centred also norm_part[b * pstride + 1] = sum((y_in - mean)^2).
+// y_in may equal y_out (each thread reads its rows before writing them).
+// When taken is non-null and the update ran, taken[0] += 1, taken[1] += ncols.
 int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    const float* coef, const float* mean_sum, uint64_t n,
                    const float* y_in, float* y_out, uint64_t nblocks,
-                   float* norm_part, uint32_t pstride, cudaStream_t s);
+                   float* norm_part, uint32_t pstride, cudaStream_t s,
+                   bool with_centred = false, const float* gate = nullptr,
+                   unsigned long long* taken = nullptr);
 
 // CGS2 middle pass in one read of U: y_out = y_in - (mean + U[:, :ncols] coef)
 // as launch_uupdate, and part[b * pstride + c] = U[rows of b, c] . y_out[rows
@@ -35,7 +45,8 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
 // out[c] = sum_b part[b * pstride + c] (coalesced: lanes take columns, warps
 // stride the blocks; the warp sums are added in warp order).
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
-                       uint32_t ncols, float* out, cudaStream_t s);
+                       uint32_t ncols, float* out, cudaStream_t s,
+                       const float* gate = nullptr);
 
 // alpha = max(sqrt(sum_b part[b*pstride]), 1e-8) (FP64 sum); B[j,j] = alpha;
 // writes alpha (float) and 1/alpha (float) to scal[0], scal[1].
@@ -45,8 +56,9 @@ int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
 
 // V-side half step (pca.pyx:1103-1171): given z = (X^T u) / sd, forms
 // z - alpha V[:, j], runs `passes` rounds of classical Gram-Schmidt against
-// V[:, :j+1]; then either V[:, j+1] = z / beta, B[j, j+1] = beta (j < m-1)
-// or rem = z (j == m-1).
+// V[:, :j+1] (passes = 0: one round, and a second only when the first kept
+// less than half of the squared norm); then either V[:, j+1] = z / beta,
+// B[j, j+1] = beta (j < m-1) or rem = z (j == m-1).
 int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
                  uint32_t j, uint32_t m, const float* scal, double* B,
                  float* rem, int passes, cudaStream_t s);

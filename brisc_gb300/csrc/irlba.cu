@@ -157,13 +157,14 @@ struct Solver {
   uint64_t ldu, ldv, nb;
   uint32_t ps;
   int passes;
+  bool adaptive;  // second U-side pass only where the first cancelled
   cudaStream_t s;
   float tol;
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
       Vbt, Ub2, Vbt2, gram, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
       sb64, ratios,
-      derr;
+      derr, taken;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
   int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
@@ -171,6 +172,7 @@ struct Solver {
 
   // accounting
   uint64_t launches = 0;
+  uint64_t second_host = 0;  // second passes of a fixed-CGS2 solve
   double reorth_bytes = 0, rotation_bytes = 0;
   // profiling: event pairs around each kernel class, in two pools that
   // alternate by restart: a restart's events are read on the host while the
@@ -230,6 +232,7 @@ struct Solver {
     nb = ceil_div(n, kRowBlock);
     ps = m + 2;
     passes = o.reorth_passes == 1 ? 1 : 2;
+    adaptive = o.reorth_passes == 0;
   }
 
   int alloc() {
@@ -264,6 +267,7 @@ struct Solver {
     BGPU_TRY(balloc(st, sizeof(RestartStatus), true, s));
     BGPU_TRY(balloc(sdpart, (size_t)X.num_panels * g * 16, false, s));
     BGPU_TRY(balloc(svdinfo, 16, true, s));
+    BGPU_TRY(balloc(taken, 16, true, s));
     return BGPU_OK;
   }
 
@@ -299,13 +303,33 @@ struct Solver {
       BGPU_TRY(launch_udots(Up, ldu, j, y0p, nb, partp, ps, true, s));
       BGPU_TRY(launch_reduce_cols(partp, nb, ps, j + 1, coefp, s));
       launches += 2;
-      // algorithmic U-pass bytes (dots + update per pass): 2 n j 4 passes
-      reorth_bytes += 2.0 * j * passes * col;
+      // algorithmic U-pass bytes (dots + update per pass): 2 n j 4 passes;
+      // an adaptive solve adds its second passes from the device count at
+      // the end
+      reorth_bytes += 2.0 * j * (adaptive ? 1 : passes) * col;
       if (passes == 1) {
         BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
                                 partp, ps, s));
         launches += 1;
         yfin = y1p;
+      } else if (adaptive) {
+        // One pass in place, as the reference (y0 <- y0 - (mean + U c1)),
+        // with the block sums of |y1|^2 and |y0 - mean|^2; their totals are
+        // the gate. The second pass (dots, reduce, update, in place) runs
+        // only where the first kept less than half of the squared norm; its
+        // kernels return at once otherwise, and the first pass's norm
+        // partials stand for finish_norm.
+        float* gate = coef2 + m;  // past the second pass's j <= m - 1 dots
+        BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y0p, nb,
+                                partp, ps, s, true));
+        BGPU_TRY(launch_reduce_cols(partp, nb, ps, 2, gate, s));
+        BGPU_TRY(launch_udots(Up, ldu, j, y0p, nb, partp, ps, false, s, gate));
+        BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s, gate));
+        BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y0p, y0p, nb,
+                                partp, ps, s, false, gate,
+                                taken.as<unsigned long long>()));
+        launches += 5;
+        yfin = y0p;
       } else {
         if (uupdate_dots_smem(j) <= 227 * 1024) {
           BGPU_TRY(launch_uupdate_dots(Up, ldu, j, coefp, coefp + j, n, y0p, y1p,
@@ -319,6 +343,7 @@ struct Solver {
         }
         BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y1p, y0p, nb,
                                 partp, ps, s));
+        ++second_host;
         launches += 4;
         yfin = y0p;
       }
@@ -339,7 +364,8 @@ struct Solver {
     BGPU_TRY(ev_end());
     BGPU_TRY(ev_begin(4));
     BGPU_TRY(launch_vstep(zvec.as<float>(), V.as<float>(), ldv, g, j, m, scalp,
-                          B.as<double>(), rem.as<float>(), passes, s));
+                          B.as<double>(), rem.as<float>(), adaptive ? 0 : passes,
+                          s));
     BGPU_TRY(ev_end());
     launches += 3;
     return BGPU_OK;
@@ -513,7 +539,11 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     BGPU_CUDA(cudaMemcpyAsync(loadings, ldev.p, (size_t)g * k * 4,
                               cudaMemcpyDeviceToHost, s));
   }
+  unsigned long long taken[2] = {0, 0};
+  if (S.adaptive)
+    BGPU_CUDA(cudaMemcpyAsync(taken, S.taken.p, sizeof(taken), cudaMemcpyDeviceToHost, s));
   BGPU_CUDA(cudaStreamSynchronize(s));
+  S.reorth_bytes += 2.0 * (double)taken[1] * (double)S.n * 4.0;
   BGPU_TRY(S.ev_collect(0));  // whatever the last restarts left in the pools
   BGPU_TRY(S.ev_collect(1));
   if (info) {
@@ -536,6 +566,7 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     info->reorth_bytes = S.reorth_bytes;
     info->rotation_bytes = S.rotation_bytes;
     info->kernel_launches = S.launches + 1 + (loadings ? 1 : 0);
+    info->second_passes = S.adaptive ? taken[0] : S.second_host;
   }
   return BGPU_OK;
 }
@@ -563,7 +594,7 @@ extern "C" void bgpu_solve_opts_default(bgpu_solve_opts* o) {
   o->max_iterations = 100;
   o->seed = 0;
   o->chunk_size = 1024;
-  o->reorth_passes = 2;
+  o->reorth_passes = 0;
   o->rotation_mode = 0;
   o->cancel = nullptr;
   o->use_graphs = 0;

@@ -216,7 +216,8 @@ class DeviceMatrix:
 
     def solve(self, num_PCs: int = 50, subspace_size: int = 100,
               tolerance: float = 1e-6, max_iterations: int = 100,
-              seed: int = 0, chunk_size: int = 1024, *, reorth_passes: int = 2,
+              seed: int = 0, chunk_size: int = 1024, *,
+              reorth_passes: int | str = "auto",
               rotation_mode: int = 0, loadings: bool = False, PCs=None,
               use_graphs: bool = False, profile: bool = False,
               svd_fp64: bool = False, stream=None) -> SolveResult:
@@ -225,7 +226,8 @@ class DeviceMatrix:
         o.k, o.subspace_size = int(num_PCs), int(subspace_size)
         o.tolerance, o.max_iterations = float(tolerance), int(max_iterations)
         o.seed, o.chunk_size = int(seed) & 0xFFFFFFFFFFFFFFFF, int(chunk_size)
-        o.reorth_passes, o.rotation_mode = int(reorth_passes), int(rotation_mode)
+        o.reorth_passes = reorth_code(reorth_passes)
+        o.rotation_mode = int(rotation_mode)
         o.use_graphs, o.profile = int(use_graphs), int(profile)
         o.svd_fp64 = int(svd_fp64)
         on_dev = PCs is not None and not isinstance(PCs, np.ndarray)
@@ -237,6 +239,18 @@ class DeviceMatrix:
         L.call("bgpu_irlba", self.handle, C.byref(o), _ptr(PCs), int(on_dev),
                sv.ctypes.data, _ptr(ld), C.byref(info), _stream(stream))
         return SolveResult(PCs, sv, ld, bool(info.converged), info.as_dict())
+
+
+def reorth_code(reorth_passes) -> int:
+    """U-side Gram-Schmidt passes per Lanczos step: "auto" (one pass as the
+    reference, a second only where the first cancelled more than half of the
+    squared norm), 1 or 2."""
+    if isinstance(reorth_passes, str):
+        if reorth_passes == "auto":
+            return 0
+    elif reorth_passes in (1, 2):
+        return int(reorth_passes)
+    raise ValueError(f"reorth_passes must be 'auto', 1 or 2, got {reorth_passes!r}")
 
 
 def _np_dtype(a) -> np.dtype:

@@ -139,8 +139,14 @@ typedef struct bgpu_solve_opts {
   uint64_t seed;             /* PCG32 seed of the start vector                   */
   uint64_t chunk_size;       /* accepted for signature parity: the GPU reduces
                                 over fixed 1024-row blocks whatever its value   */
-  uint32_t reorth_passes;    /* 1 = classical Gram-Schmidt as the reference,
-                                2 = CGS2 (default when 0)                        */
+  uint32_t reorth_passes;    /* U-side Gram-Schmidt per Lanczos step:
+                                0 = adaptive (default): one classical pass as
+                                the reference, and a second one only at steps
+                                where the first removed more than half of the
+                                vector's squared norm ("twice is enough",
+                                Kahan-Parlett); 1 = one pass always;
+                                2 = two passes always (CGS2). The V side
+                                follows the same rule.                          */
   uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor cores
                                 when subspace_size <= 104, else SIMT),
                                 1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass TF32
@@ -178,6 +184,7 @@ typedef struct bgpu_solve_info {
                                 Gram-Schmidt pass and step                     */
   double rotation_bytes;     /* summed (n + g)(m + kc) 4 of the restart rotations */
   uint64_t kernel_launches;  /* kernels launched by this solve                    */
+  uint64_t second_passes;    /* Lanczos steps that ran a second U-side pass       */
 } bgpu_solve_info;
 
 BGPU_API void bgpu_solve_opts_default(bgpu_solve_opts* opts);

@@ -10,7 +10,9 @@ and the final PCs (pca.pyx:1239-1255).
 
 Knobs that the GPU implementation exposes are mirrored so the checker can
 model it: ``reorth_passes`` (1 = the reference's single classical
-Gram-Schmidt pass, 2 = CGS2) and ``sd`` (the per-gene std to use). When
+Gram-Schmidt pass, 2 = CGS2, 0 = the GPU's adaptive mode: on either side a
+second pass only at steps where the first kept less than half of the squared
+norm) and ``sd`` (the per-gene std to use). When
 ``max_iterations`` runs out without convergence, the reference rotates U once
 more and then multiplies by Ub again, reading buffer columns left from an
 earlier restart (pca.pyx:1210-1215, 1253); those contents are not defined by
@@ -56,7 +58,7 @@ def irlba(X, k: int = 50, subspace_size: int = 100, tolerance: float = 1e-6,
     rem = np.zeros(g, dtype=F32)
     kc, smax, converged = 0, F32(2.4221817809573368e-05), False
     Ub = Sb = Vbt = None
-    restarts = steps = 0
+    restarts = steps = second_passes = second_passes_v = 0
     for it in range(max_iterations):
         j = kc
         while True:
@@ -65,8 +67,13 @@ def irlba(X, k: int = 50, subspace_size: int = 100, tolerance: float = 1e-6,
             if j > 0:                                          # pca.pyx:997-1052
                 Uj = U[:, :j]
                 w = (Uj.T @ y).astype(F32)
+                y0c = (y - mean).astype(F32)
                 y = (y - (mean + Uj @ w)).astype(F32)
-                for _ in range(reorth_passes - 1):
+                second = reorth_passes == 2 or (
+                    reorth_passes == 0
+                    and F32(np.dot(y, y)) < F32(0.5) * F32(np.dot(y0c, y0c)))
+                second_passes += int(second)
+                for _ in range(1 if second else 0):
                     w = (Uj.T @ y).astype(F32)
                     y = (y - Uj @ w).astype(F32)
             else:                                              # pca.pyx:1053-1079
@@ -78,7 +85,12 @@ def irlba(X, k: int = 50, subspace_size: int = 100, tolerance: float = 1e-6,
             z = ((Xt @ U[:, j]) / sd).astype(F32)              # pca.pyx:1096-1101
             z = (z - alpha * V[:, j]).astype(F32)
             Vj = V[:, :j + 1]
-            for _ in range(reorth_passes):                     # pca.pyx:1114-1128
+            z0 = z
+            for p in range(1 if reorth_passes == 1 else 2):    # pca.pyx:1114-1128
+                if p == 1 and reorth_passes == 0:
+                    if F32(np.dot(z, z)) >= F32(0.5) * F32(np.dot(z0, z0)):
+                        break
+                    second_passes_v += 1
                 w = (Vj.T @ z).astype(F32)
                 z = (z - Vj @ w).astype(F32)
             steps += 1
@@ -116,4 +128,5 @@ def irlba(X, k: int = 50, subspace_size: int = 100, tolerance: float = 1e-6,
     PCs = np.ascontiguousarray(U @ W, dtype=F32)               # pca.pyx:1249-1254
     loadings = np.ascontiguousarray(V @ Vbt[:k, :m].T, dtype=F32)
     return dict(PCs=PCs, S=np.asarray(Sb[:k], dtype=F32), loadings=loadings,
-                converged=converged, restarts=restarts, steps=steps, sd=sd)
+                converged=converged, restarts=restarts, steps=steps, sd=sd,
+                second_passes=second_passes, second_passes_v=second_passes_v)

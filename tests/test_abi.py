@@ -70,7 +70,7 @@ def test_invalid_arguments_rejected_without_gpu(built_lib):
     o = _lib.SolveOpts()
     L.bgpu_solve_opts_default(C.byref(o))
     assert (o.k, o.subspace_size, o.max_iterations) == (50, 100, 100)
-    assert abs(o.tolerance - 1e-6) < 1e-12 and o.reorth_passes == 2
+    assert abs(o.tolerance - 1e-6) < 1e-12 and o.reorth_passes == 0
     assert L.bgpu_irlba(None, C.byref(o), None, 0, None, None, None, None) == _lib.ERR_INVALID
     d = _lib.MatrixDesc()
     d.num_cells, d.num_genes = 10, 70000

@@ -94,10 +94,12 @@ def test_bit_identical_runs(cuda, golden):
     assert np.array_equal(a.singular_values, c.singular_values)
 
 
-@pytest.mark.parametrize("passes,rotation", [(1, 0), (2, 0), (2, 1), (2, 2)])
+@pytest.mark.parametrize("passes,rotation",
+                         [("auto", 0), (1, 0), (2, 0), (2, 1), (2, 2)])
 def test_reorth_passes_both_meet_gates(cuda, golden, passes, rotation):
-    """Both Gram-Schmidt modes and both restart rotations (SIMT FP32 and the
-    tensor-core 3-pass TF32 split) meet the FP64 gates."""
+    """Every Gram-Schmidt mode (adaptive, one pass, CGS2) and both restart
+    rotations (SIMT FP32 and the tensor-core 3-pass TF32 split) meet the FP64
+    gates."""
     z = golden("irlba")
     X, n, g, k, m = _case(z, "clustered_b")
     M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
@@ -237,3 +239,55 @@ def test_large_solve_meets_fp64_gate(cuda):
     S64 = dense.top_svd(X, 52)[0]
     assert r.converged
     assert dense.rel_sv_error(r.PCs, S64).max() < 1e-4
+
+
+def _near_low_rank(seed=0, n=4000, g=400, rank=8):
+    rng = np.random.default_rng(seed)
+    W = rng.random((n, rank)) * (rng.random((n, rank)) < 0.3)
+    H = rng.random((rank, g)) * (rng.random((rank, g)) < 0.5)
+    A = W @ H
+    A = A + 1e-3 * rng.random((n, g)) * (A > 0)
+    return sp.csr_matrix(A.astype(np.float32))
+
+
+def test_adaptive_second_pass_where_first_cancels(cuda):
+    """On a near-low-rank matrix the first Gram-Schmidt pass cancels most of
+    X.v at some steps; the adaptive mode runs the second pass at exactly the
+    steps where the oracle's FP32 norms say so and meets the FP64 gates.
+    A fixed-CGS2 solve reports a second pass at every step past the first."""
+    X = _near_low_rank()
+    n, g = X.shape
+    k, m = 6, 16
+    o = oirlba.irlba(X, k, m, reorth_passes=0)
+    assert 0 < o["second_passes"] < o["steps"] - 1
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    r = M.solve(k, m)
+    r2 = M.solve(k, m, reorth_passes=2)
+    M.close()
+    assert r.info["lanczos_steps"] == o["steps"]
+    assert r.info["second_passes"] == o["second_passes"]
+    assert r2.info["second_passes"] == r2.info["lanczos_steps"] - 1
+    S, U, Vt = dense.top_svd(X, k + 2)
+    assert r.converged
+    assert dense.rel_sv_error(r.PCs, S).max() < 1e-4
+    # the adaptive solve reads U fewer times than CGS2
+    assert r.info["reorth_bytes"] < r2.info["reorth_bytes"]
+
+
+@pytest.mark.parametrize("name", ["clustered_a", "clustered_b", "flat"])
+def test_adaptive_equals_single_pass_when_no_cancellation(cuda, golden, name):
+    """Where no step cancels (the oracle takes no second pass on either
+    side), the adaptive mode is the reference's single pass bit for bit: the
+    first pass is the same kernel sequence and the gated kernels write
+    nothing."""
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, name)
+    o = oirlba.irlba(X, k, m, reorth_passes=0)
+    assert o["second_passes"] == 0 and o["second_passes_v"] == 0
+    M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+    a = M.solve(k, m)
+    b = M.solve(k, m, reorth_passes=1)
+    M.close()
+    assert a.info["second_passes"] == 0
+    assert np.array_equal(a.PCs, b.PCs)
+    assert np.array_equal(a.singular_values, b.singular_values)

@@ -74,3 +74,11 @@ def test_generator_clusters():
     c = nb_counts(5000, 100, seed=2, density=0.08, clusters=13, workers=1)
     assert c.clusters is not None and c.clusters.shape[0] == c.num_cells
     assert set(np.unique(c.clusters)) <= set(range(13))
+
+
+def test_reorth_modes():
+    from brisc_gb300.pca import reorth_code
+    assert (reorth_code("auto"), reorth_code(1), reorth_code(2)) == (0, 1, 2)
+    for bad in (0, 3, "two", None, 1.5):
+        with pytest.raises(ValueError, match="reorth_passes"):
+            reorth_code(bad)

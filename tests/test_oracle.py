@@ -72,12 +72,16 @@ def _case(z, name):
     return X, k, m
 
 
+@pytest.mark.parametrize("passes", [1, 0])
 @pytest.mark.parametrize("name", ["clustered_a", "clustered_b"])
-def test_oracle_irlba_matches_reference(golden, name):
+def test_oracle_irlba_matches_reference(golden, name, passes):
+    """The reference's single pass, and the adaptive mode (a second U-side
+    pass only where the first cancels, two V-side passes), both agree with
+    the reference's own PCs."""
     z = golden("irlba")
     X, k, m = _case(z, name)
     ref_pcs = z[f"{name}_pcs"]
-    o = oirlba.irlba(X, k, m)
+    o = oirlba.irlba(X, k, m, reorth_passes=passes)
     assert o["converged"] == bool(z[f"{name}_converged"])
     s_ref = dense.sv_from_pcs(ref_pcs)
     s_or = dense.sv_from_pcs(o["PCs"])
