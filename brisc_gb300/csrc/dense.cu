@@ -31,12 +31,21 @@ __device__ __forceinline__ bool second_pass_skipped(const float* gate) {
   return gate != nullptr && gate[0] >= 0.5f * gate[1];
 }
 
-__global__ void __launch_bounds__(256)
+// Per-warp column sums go to shared memory ([warp][column], no block barrier
+// per chunk, so a warp's next 16 loads issue while the others reduce); one
+// barrier at the end, then part[b][c] = the 8 warp sums in warp order.
+// __launch_bounds__(256, 8): 32 registers, so the 1024-row blocks of a
+// million-cell basis (977) all run in one wave (8 per SM, 2048 threads, each
+// with kDotCols 16-byte loads in flight).
+constexpr int kDotCols = 4;
+
+__global__ void __launch_bounds__(256, 8)
 k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
         const float* __restrict__ y, float* __restrict__ part,
         uint32_t pstride, int with_sum, const float* __restrict__ gate) {
   if (second_pass_skipped(gate)) return;
-  __shared__ float red[8][9];
+  extern __shared__ float wsum[];  // 8 x (ncols + 1)
+  const uint32_t ld = ncols + 1;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint64_t b = blockIdx.x;
   const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
@@ -44,19 +53,13 @@ k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   const float4 yv = in ? *reinterpret_cast<const float4*>(y + row0)
                        : make_float4(0.f, 0.f, 0.f, 0.f);
   if (with_sum) {
-    float s = warp_sum(yv.x + yv.y + yv.z + yv.w);
-    if (lane == 0) red[wid][8] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float t = 0.f;
-      for (int w = 0; w < 8; ++w) t += red[w][8];
-      part[b * pstride + ncols] = t;
-    }
+    const float s = warp_sum(yv.x + yv.y + yv.z + yv.w);
+    if (lane == 0) wsum[wid * ld + ncols] = s;
   }
-  for (uint32_t c0 = 0; c0 < ncols; c0 += 8) {
-    float acc[8];
+  for (uint32_t c0 = 0; c0 < ncols; c0 += kDotCols) {
+    float acc[kDotCols];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kDotCols; ++k) {
       const uint32_t c = c0 + k;
       acc[k] = 0.f;
       if (in && c < ncols) {
@@ -65,22 +68,24 @@ k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
       }
     }
 #pragma unroll
-    for (int k = 0; k < 8; ++k) acc[k] = warp_sum(acc[k]);
+    for (int k = 0; k < kDotCols; ++k) acc[k] = warp_sum(acc[k]);
     if (lane == 0) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) red[wid][k] = acc[k];
+      for (int k = 0; k < kDotCols; ++k)
+        if (c0 + k < ncols) wsum[wid * ld + c0 + k] = acc[k];
     }
-    __syncthreads();
-    if (threadIdx.x < 8 && c0 + threadIdx.x < ncols) {
-      float t = 0.f;
-      for (int w = 0; w < 8; ++w) t += red[w][threadIdx.x];
-      part[b * pstride + c0 + threadIdx.x] = t;
-    }
-    __syncthreads();
+  }
+  __syncthreads();
+  const uint32_t nout = ncols + (with_sum ? 1u : 0u);
+  for (uint32_t c = threadIdx.x; c < nout; c += blockDim.x) {
+    float t = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += wsum[w * ld + c];
+    part[b * pstride + c] = t;
   }
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)  // one wave, as k_udots
 k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
           const float* __restrict__ coef, const float* __restrict__ mean_sum,
           uint64_t n, const float* y_in, float* y_out,  // may be the same
@@ -109,7 +114,7 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
       sqc = cx * cx + cy * cy + cz * cz + cw * cw;
     }
     float4 t = make_float4(mean, mean, mean, mean);
-#pragma unroll 8
+#pragma unroll 4
     for (uint32_t c = 0; c < ncols; ++c) {
       const float4 u = __ldcs(reinterpret_cast<const float4*>(U + c * ldu + row0));
       const float w = cs[c];
@@ -522,8 +527,11 @@ __global__ void k_b_to_float(const double* __restrict__ B, uint64_t count,
 int launch_udots(const float* U, uint64_t ldu, uint32_t ncols, const float* y,
                  uint64_t nblocks, float* part, uint32_t pstride, bool with_sum,
                  cudaStream_t s, const float* gate) {
-  k_udots<<<(unsigned)nblocks, 256, 0, s>>>(U, ldu, ncols, y, part, pstride,
-                                            with_sum ? 1 : 0, gate);
+  const size_t smem = 8ull * (ncols + 1) * sizeof(float);
+  BGPU_REQUIRE(smem <= 227 * 1024, BGPU_ERR_UNSUPPORTED, "U dots: too many columns");
+  if (smem > 48 * 1024) BGPU_CUDA(allow_max_smem(k_udots));
+  k_udots<<<(unsigned)nblocks, 256, smem, s>>>(U, ldu, ncols, y, part, pstride,
+                                               with_sum ? 1 : 0, gate);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
