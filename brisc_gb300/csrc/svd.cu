@@ -12,6 +12,7 @@
 // the Lanczos steps it serves; the reference itself uses FP32 (sgesdd).
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "svd.cuh"
 
@@ -59,11 +60,34 @@ __device__ __forceinline__ void rotation_of(double al, double be, double ga, dou
   *tan_out = t;
 }
 
+// Column stride of A (len m + 1) and J (len m) in the workspace. The FP32
+// kernel pads columns to a multiple of 32 floats so each lane of a pair's
+// 8-lane group moves whole float4s (a group covers 128 contiguous bytes per
+// access: no bank conflicts, a quarter of the shared-memory instructions);
+// the padding is zero and stays zero under rotations.
+template <typename T>
+__host__ __device__ constexpr uint32_t col_stride(uint32_t len) {
+  return std::is_same<T, float>::value ? (len + 31u) & ~31u : len;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum_t(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Rotates the float4 columns x, y (nv vectors each) of one pair: an 8-lane
+// group, lane l8 taking vectors l8, l8 + 8, ...
+__device__ __forceinline__ void rotate_cols4(float4* x, float4* y, uint32_t nv,
+                                             int l8, float c, float sn) {
+  for (uint32_t v = l8; v < nv; v += 8) {
+    const float4 a = x[v], b = y[v];
+    x[v] = make_float4(c * a.x - sn * b.x, c * a.y - sn * b.y, c * a.z - sn * b.z,
+                       c * a.w - sn * b.w);
+    y[v] = make_float4(sn * a.x + c * b.x, sn * a.y + c * b.y, sn * a.z + c * b.z,
+                       sn * a.w + c * b.w);
+  }
 }
 
 // T = float (FP32 Jacobi) or double (FP64 Jacobi). B is read in T; outputs are
@@ -81,15 +105,18 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int la = (int)m + 1;  // column length of A = B^T
+  const uint32_t lp = col_stride<T>(m + 1), jd = col_stride<T>(m);
   T* A = use_smem ? reinterpret_cast<T*>(smraw) : gwork;
-  T* J = A + (uint64_t)m * la;
-  T* sig = J + (uint64_t)m * m;
-  for (uint32_t t = threadIdx.x; t < m * (uint32_t)la; t += blockDim.x) {
-    const uint32_t i = t / la, r = t % la;   // A[r, i] = B[i, r]
-    A[(uint64_t)i * la + r] = Bin[i + (uint64_t)r * m];
+  T* J = A + (uint64_t)m * lp;
+  T* sig = J + (uint64_t)m * jd;
+  for (uint32_t t = threadIdx.x; t < m * lp; t += blockDim.x) {
+    const uint32_t i = t / lp, r = t % lp;   // A[r, i] = B[i, r]
+    A[t] = r < (uint32_t)la ? Bin[i + (uint64_t)r * m] : T(0);
   }
-  for (uint32_t t = threadIdx.x; t < m * m; t += blockDim.x)
-    J[t] = (t / m == t % m) ? T(1) : T(0);
+  for (uint32_t t = threadIdx.x; t < m * jd; t += blockDim.x) {
+    const uint32_t i = t / jd, r = t % jd;
+    J[t] = r == i ? T(1) : T(0);
+  }
   __syncthreads();
 
   // Pairs go to 8-lane groups (up to 128 disjoint pairs per round at once):
@@ -107,7 +134,7 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) rotated = 0;
     for (uint32_t i = wid; i < m; i += nw) {
-      const T* ai = A + (uint64_t)i * la;
+      const T* ai = A + (uint64_t)i * lp;
       T t2 = 0;
       for (int r = lane; r < la; r += 32) t2 += ai[r] * ai[r];
       t2 = warp_sum_t(t2);
@@ -119,11 +146,25 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
         int p, q;
         pair_of(round, idx, M2, &p, &q);
         if (q >= (int)m) continue;
-        T* ap = A + (uint64_t)p * la;
-        T* aq = A + (uint64_t)q * la;
+        T* ap = A + (uint64_t)p * lp;
+        T* aq = A + (uint64_t)q * lp;
+        T* jp = J + (uint64_t)p * jd;
+        T* jq = J + (uint64_t)q * jd;
         const T al = nrm[p], be = nrm[q];
         T ga = 0;
-        for (int r = l8; r < la; r += 8) ga += ap[r] * aq[r];
+        if constexpr (std::is_same<T, float>::value) {
+          const float4* apv = reinterpret_cast<const float4*>(ap);
+          const float4* aqv = reinterpret_cast<const float4*>(aq);
+          for (uint32_t v = l8; v < lp / 4; v += 8) {
+            const float4 x = apv[v], y = aqv[v];
+            ga += x.x * y.x;
+            ga += x.y * y.y;
+            ga += x.z * y.z;
+            ga += x.w * y.w;
+          }
+        } else {
+          for (int r = l8; r < la; r += 8) ga += ap[r] * aq[r];
+        }
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) ga += __shfl_xor_sync(gm8, ga, o);
         if (al > T(0) && be > T(0) && ga * ga > thresh * thresh * (al * be)) {
@@ -133,17 +174,22 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
             nrm[p] = al - tn * ga;
             nrm[q] = be + tn * ga;
           }
-          for (int r = l8; r < la; r += 8) {
-            const T x = ap[r], y = aq[r];
-            ap[r] = c * x - sn * y;
-            aq[r] = sn * x + c * y;
-          }
-          T* jp = J + (uint64_t)p * m;
-          T* jq = J + (uint64_t)q * m;
-          for (int r = l8; r < (int)m; r += 8) {
-            const T x = jp[r], y = jq[r];
-            jp[r] = c * x - sn * y;
-            jq[r] = sn * x + c * y;
+          if constexpr (std::is_same<T, float>::value) {
+            rotate_cols4(reinterpret_cast<float4*>(ap), reinterpret_cast<float4*>(aq),
+                         lp / 4, l8, c, sn);
+            rotate_cols4(reinterpret_cast<float4*>(jp), reinterpret_cast<float4*>(jq),
+                         jd / 4, l8, c, sn);
+          } else {
+            for (int r = l8; r < la; r += 8) {
+              const T x = ap[r], y = aq[r];
+              ap[r] = c * x - sn * y;
+              aq[r] = sn * x + c * y;
+            }
+            for (int r = l8; r < (int)m; r += 8) {
+              const T x = jp[r], y = jq[r];
+              jp[r] = c * x - sn * y;
+              jq[r] = sn * x + c * y;
+            }
           }
           if (l8 == 0) rotated = 1;
         }
@@ -157,7 +203,7 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
 
   // singular values, descending order (ties by index), vectors
   for (uint32_t i = wid; i < m; i += nw) {
-    const T* ai = A + (uint64_t)i * la;
+    const T* ai = A + (uint64_t)i * lp;
     T t = 0;
     for (int r = lane; r < la; r += 32) t += ai[r] * ai[r];
     t = warp_sum_t(t);
@@ -173,14 +219,14 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rank += __shfl_xor_sync(0xffffffffu, rank, o);
-    const T* ji = J + (uint64_t)i * m;
+    const T* ji = J + (uint64_t)i * jd;
     if (lane == 0) {
       Sb[rank] = (float)si;
       if (sb64) sb64[rank] = (double)si;
       if (ub_last) ub_last[rank] = (double)ji[m - 1];
     }
     for (uint32_t r = lane; r < m; r += 32) Ub[r + (uint64_t)rank * m] = (float)ji[r];
-    const T* ai = A + (uint64_t)i * la;
+    const T* ai = A + (uint64_t)i * lp;
     const T inv = si > T(0) ? T(1) / si : T(0);
     for (int r = lane; r < la; r += 32)
       Vbt[rank + (uint64_t)r * m] = (float)(ai[r] * inv);
@@ -315,7 +361,9 @@ int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s
 }
 
 size_t jacobi_smem_bytes(uint32_t m, bool fp64) {
-  return ((size_t)m * (m + 1) + (size_t)m * m + m) * (fp64 ? 8 : 4);
+  if (fp64)
+    return ((size_t)m * col_stride<double>(m + 1) + (size_t)m * col_stride<double>(m) + m) * 8;
+  return ((size_t)m * col_stride<float>(m + 1) + (size_t)m * col_stride<float>(m) + m) * 4;
 }
 
 size_t jacobi_global_bytes(uint32_t m, bool fp64) {
