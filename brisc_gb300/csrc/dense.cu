@@ -85,12 +85,54 @@ k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   }
 }
 
+// alpha = max(sqrt(sum_b part[b * pstride]), 1e-8) in FP64 (clip_val,
+// pca.pyx:1084-1086); B[j, j] = alpha, scal = {alpha, 1 / alpha}; with_centred:
+// gate = {sum of column 0, sum of column 1}. One 256-thread block, each
+// thread summing blocks tid, tid + 256, ... then a fixed shuffle tree and the
+// warps in order. Partials written by other blocks are read through L2.
+__device__ void finish_norm_block(const float* part, uint64_t nblocks,
+                                  uint32_t pstride, int with_centred,
+                                  const NormFinish& fin) {
+  __shared__ double dred[2][8];
+  double t = 0.0, tc = 0.0;
+  for (uint64_t b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    t += (double)__ldcg(part + b * pstride);
+    if (with_centred) tc += (double)__ldcg(part + b * pstride + 1);
+  }
+  t = warp_sum(t);
+  tc = warp_sum(tc);
+  if ((threadIdx.x & 31) == 0) {
+    dred[0][threadIdx.x >> 5] = t;
+    dred[1][threadIdx.x >> 5] = tc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, sc = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      s += dred[0][w];
+      sc += dred[1][w];
+    }
+    double a = sqrt(s);
+    if (a < 1e-8) a = 1e-8;  // clip_val, pca.pyx:1084-1085
+    fin.B[fin.j + (uint64_t)fin.j * fin.m] = a;
+    const float af = (float)a;
+    fin.scal[0] = af;
+    fin.scal[1] = 1.f / af;  // inverse_alpha, pca.pyx:1086
+    if (fin.gate) {
+      fin.gate[0] = (float)s;
+      fin.gate[1] = (float)sc;
+    }
+    *fin.counter = 0u;  // every block has taken its ticket
+  }
+}
+
 __global__ void __launch_bounds__(256, 8)  // one wave, as k_udots
 k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
           const float* __restrict__ coef, const float* __restrict__ mean_sum,
           uint64_t n, const float* y_in, float* y_out,  // may be the same
           float* __restrict__ norm_part, uint32_t pstride, int with_centred,
-          const float* __restrict__ gate, unsigned long long* __restrict__ taken) {
+          const float* __restrict__ gate, unsigned long long* __restrict__ taken,
+          NormFinish fin) {
   if (second_pass_skipped(gate)) return;
   if (taken && blockIdx.x == 0 && threadIdx.x == 0) {
     taken[0] += 1ull;
@@ -142,6 +184,19 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
       float t = 0.f;
       for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
       norm_part[b * pstride + threadIdx.x] = t;
+    }
+    if (fin.B) {
+      // The block that finishes last (one atomic ticket per block, no
+      // waiting) sums every block's partials, in block order whichever
+      // block it is.
+      __shared__ bool last;
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) last = atomicAdd(fin.counter, 1u) == gridDim.x - 1;
+      __syncthreads();
+      if (!last) return;
+      __threadfence();
+      finish_norm_block(norm_part, gridDim.x, pstride, with_centred, fin);
     }
   }
 }
@@ -233,29 +288,6 @@ k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride
     float r = 0.f;
     for (int w = 0; w < 32; ++w) r += ws[w][lane];
     out[c] = r;
-  }
-}
-
-__global__ void __launch_bounds__(256)
-k_finish_norm(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
-              double* __restrict__ B, uint32_t m, uint32_t j,
-              float* __restrict__ scal) {
-  __shared__ double red[8];
-  double t = 0.0;
-  for (uint64_t b = threadIdx.x; b < nblocks; b += blockDim.x)
-    t += (double)part[b * pstride];
-  t = warp_sum(t);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < 8; ++w) s += red[w];
-    double a = sqrt(s);
-    if (a < 1e-8) a = 1e-8;  // clip_val, pca.pyx:1084-1085
-    B[j + (uint64_t)j * m] = a;
-    const float af = (float)a;
-    scal[0] = af;
-    scal[1] = 1.f / af;  // inverse_alpha, pca.pyx:1086
   }
 }
 
@@ -541,10 +573,12 @@ int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    const float* y_in, float* y_out, uint64_t nblocks,
                    float* norm_part, uint32_t pstride, cudaStream_t s,
                    bool with_centred, const float* gate,
-                   unsigned long long* taken) {
+                   unsigned long long* taken, NormFinish fin) {
+  BGPU_REQUIRE(!fin.B || (norm_part && fin.counter && fin.scal), BGPU_ERR_INVALID,
+               "U update: norm finish needs partials, a ticket counter and scal");
   k_uupdate<<<(unsigned)nblocks, 256, std::max<size_t>(ncols, 1) * 4, s>>>(
       U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride,
-      with_centred ? 1 : 0, gate, taken);
+      with_centred ? 1 : 0, gate, taken, fin);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -576,14 +610,6 @@ int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
   k_reduce_cols<<<(unsigned)ceil_div(ncols, 32), 1024, 0, s>>>(part, nblocks,
                                                                pstride, ncols, out,
                                                                gate);
-  BGPU_CHECK_LAUNCH();
-  return BGPU_OK;
-}
-
-int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
-                       double* B, uint32_t m, uint32_t j, float* scal,
-                       cudaStream_t s) {
-  k_finish_norm<<<1, 256, 0, s>>>(part, nblocks, pstride, B, m, j, scal);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -7,6 +7,19 @@ namespace bgpu {
 
 constexpr int kRowBlock = 1024;  // rows per fixed reduction block (256 threads x 4)
 
+// The last block of a norm-producing U update finishes the norm: B[j, j] =
+// alpha = max(sqrt(sum of the norm partials), 1e-8) in FP64 and scal =
+// {alpha, 1 / alpha} (pca.pyx:1081-1086), and, when gate
+// is non-null, gate = {|y_out|^2, |y_in - mean|^2}. counter: a zeroed device
+// word per solve (the last block resets it). B == nullptr: no finish.
+struct NormFinish {
+  double* B = nullptr;
+  uint32_t m = 0, j = 0;
+  float* scal = nullptr;
+  float* gate = nullptr;
+  unsigned* counter = nullptr;
+};
+
 // part[b * pstride + c] = U[rows of b, c] . y[rows of b]   for c < ncols
 // and, when with_sum, part[b * pstride + ncols] = sum(y[rows of b]).
 //
@@ -30,7 +43,7 @@ int launch_uupdate(const float* U, uint64_t ldu, uint32_t ncols,
                    const float* y_in, float* y_out, uint64_t nblocks,
                    float* norm_part, uint32_t pstride, cudaStream_t s,
                    bool with_centred = false, const float* gate = nullptr,
-                   unsigned long long* taken = nullptr);
+                   unsigned long long* taken = nullptr, NormFinish fin = {});
 
 // CGS2 middle pass in one read of U: y_out = y_in - (mean + U[:, :ncols] coef)
 // as launch_uupdate, and part[b * pstride + c] = U[rows of b, c] . y_out[rows
@@ -47,12 +60,6 @@ int launch_uupdate_dots(const float* U, uint64_t ldu, uint32_t ncols,
 int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
                        uint32_t ncols, float* out, cudaStream_t s,
                        const float* gate = nullptr);
-
-// alpha = max(sqrt(sum_b part[b*pstride]), 1e-8) (FP64 sum); B[j,j] = alpha;
-// writes alpha (float) and 1/alpha (float) to scal[0], scal[1].
-int launch_finish_norm(const float* part, uint64_t nblocks, uint32_t pstride,
-                       double* B, uint32_t m, uint32_t j, float* scal,
-                       cudaStream_t s);
 
 // V-side half step (pca.pyx:1103-1171): given z = (X^T u) / sd, forms
 // z - alpha V[:, j], runs `passes` rounds of classical Gram-Schmidt against

@@ -164,7 +164,7 @@ struct Solver {
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
       Vbt, Ub2, Vbt2, gram, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
       sb64, ratios,
-      derr, taken;
+      derr, taken, ticket;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
   int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
@@ -268,6 +268,7 @@ struct Solver {
     BGPU_TRY(balloc(sdpart, (size_t)X.num_panels * g * 16, false, s));
     BGPU_TRY(balloc(svdinfo, 16, true, s));
     BGPU_TRY(balloc(taken, 16, true, s));
+    BGPU_TRY(balloc(ticket, 16, true, s));
     return BGPU_OK;
   }
 
@@ -292,11 +293,20 @@ struct Solver {
     const double col = (double)n * 4.0;
     BGPU_TRY(ev_begin(3));
     float* yfin;
+    float* scalp = scal.as<float>();
+    // the last update of the step finishes the norm in its last block:
+    // B[j, j] = alpha, scal = {alpha, 1 / alpha}
+    NormFinish fin;
+    fin.B = B.as<double>();
+    fin.m = m;
+    fin.j = j;
+    fin.scal = scalp;
+    fin.counter = ticket.as<unsigned>();
     if (j == 0) {
       BGPU_TRY(launch_udots(Up, ldu, 0, y0p, nb, partp, ps, true, s));
       BGPU_TRY(launch_reduce_cols(partp, nb, ps, 1, coefp, s));
       BGPU_TRY(launch_uupdate(Up, ldu, 0, coefp, coefp, n, y0p, y1p, nb, partp,
-                              ps, s));
+                              ps, s, false, nullptr, nullptr, fin));
       launches += 3;
       yfin = y1p;
     } else {
@@ -309,47 +319,48 @@ struct Solver {
       reorth_bytes += 2.0 * j * (adaptive ? 1 : passes) * col;
       if (passes == 1) {
         BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
-                                partp, ps, s));
+                                partp, ps, s, false, nullptr, nullptr, fin));
         launches += 1;
         yfin = y1p;
       } else if (adaptive) {
         // One pass in place, as the reference (y0 <- y0 - (mean + U c1)),
-        // with the block sums of |y1|^2 and |y0 - mean|^2; their totals are
-        // the gate. The second pass (dots, reduce, update, in place) runs
-        // only where the first kept less than half of the squared norm; its
-        // kernels return at once otherwise, and the first pass's norm
-        // partials stand for finish_norm.
+        // with the block sums of |y1|^2 and |y0 - mean|^2; its last block
+        // finishes alpha and writes their totals as the gate. The second
+        // pass (dots, reduce, update, in place) runs only where the first
+        // kept less than half of the squared norm, and then finishes alpha
+        // again; its kernels return at once otherwise.
         float* gate = coef2 + m;  // past the second pass's j <= m - 1 dots
+        NormFinish fin1 = fin;
+        fin1.gate = gate;
         BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y0p, nb,
-                                partp, ps, s, true));
-        BGPU_TRY(launch_reduce_cols(partp, nb, ps, 2, gate, s));
+                                partp, ps, s, true, nullptr, nullptr, fin1));
         BGPU_TRY(launch_udots(Up, ldu, j, y0p, nb, partp, ps, false, s, gate));
         BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s, gate));
         BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y0p, y0p, nb,
                                 partp, ps, s, false, gate,
-                                taken.as<unsigned long long>()));
-        launches += 5;
+                                taken.as<unsigned long long>(), fin));
+        launches += 4;
         yfin = y0p;
       } else {
         if (uupdate_dots_smem(j) <= 227 * 1024) {
           BGPU_TRY(launch_uupdate_dots(Up, ldu, j, coefp, coefp + j, n, y0p, y1p,
                                        partp, ps, s));
           BGPU_TRY(launch_reduce_cols(partp, uupdate_dots_blocks(n), ps, j, coef2, s));
+          launches += 2;
         } else {
           BGPU_TRY(launch_uupdate(Up, ldu, j, coefp, coefp + j, n, y0p, y1p, nb,
                                   nullptr, ps, s));
           BGPU_TRY(launch_udots(Up, ldu, j, y1p, nb, partp, ps, false, s));
           BGPU_TRY(launch_reduce_cols(partp, nb, ps, j, coef2, s));
+          launches += 3;
         }
         BGPU_TRY(launch_uupdate(Up, ldu, j, coef2, nullptr, n, y1p, y0p, nb,
-                                partp, ps, s));
+                                partp, ps, s, false, nullptr, nullptr, fin));
         ++second_host;
-        launches += 4;
+        launches += 1;
         yfin = y0p;
       }
     }
-    float* scalp = scal.as<float>();
-    BGPU_TRY(launch_finish_norm(partp, nb, ps, B.as<double>(), m, j, scalp, s));
     BGPU_TRY(ev_end());
     BGPU_TRY(ev_begin(1));
     if (X.stream_ok && X.impl == 0)
@@ -367,7 +378,7 @@ struct Solver {
                           B.as<double>(), rem.as<float>(), adaptive ? 0 : passes,
                           s));
     BGPU_TRY(ev_end());
-    launches += 3;
+    launches += 2;  // reduce_panels_t, vstep
     return BGPU_OK;
   }
 };
