@@ -83,7 +83,9 @@ __device__ __noinline__ float csr_row_exact8(const uint32_t* __restrict__ packed
 // X.v, counts layout: 8 lanes per cell row.
 constexpr int kTabSlot = 17;  // padded per-group table slot (conflict-free)
 
-__global__ void __launch_bounds__(256, 4)
+constexpr int kSpmvRowsCtas = 5;  // resident CTAs per SM (48 registers)
+
+__global__ void __launch_bounds__(256, kSpmvRowsCtas)
 k_spmv_rows(CsrView X, const int32_t* __restrict__ order, const float* __restrict__ v,
             const float* __restrict__ sd, float* __restrict__ y) {
   extern __shared__ __align__(16) float sm[];
@@ -743,7 +745,7 @@ int launch_matvec_stream(const Matrix& m, const float* v, const float* sd,
   // launches a small grid and leaves the rest of the GPU to concurrent solves
   const uint64_t want = ceil_div(m.n, 32);
   const unsigned grid = (unsigned)std::max<uint64_t>(
-      1, std::min<uint64_t>(want, (uint64_t)num_sms() * 4));
+      1, std::min<uint64_t>(want, (uint64_t)num_sms() * kSpmvRowsCtas));
   k_spmv_rows<<<grid, 256, smem, s>>>(X, m.row_order, v, sd, y);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
