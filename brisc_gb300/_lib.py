@@ -16,6 +16,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libbriscgpu.so"
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_CANCELLED, ERR_DEVICE = range(7)
 INDEX_I32, INDEX_I64 = 0, 1
 VALUE_U16, VALUE_U32, VALUE_I32, VALUE_F32 = 0, 1, 2, 3
+VALUE_I64, VALUE_U64, VALUE_F64 = 4, 5, 6  # the HVG statistics only
 NORM_NONE, NORM_LOGCP10K, NORM_LOG1PPF, NORM_PFLOG1PPF = -1, 0, 1, 2
 
 
@@ -81,6 +82,25 @@ class SolveInfo(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class HvgInput(C.Structure):
+    _fields_ = [
+        ("data", C.c_void_p),
+        ("value_type", C.c_int),
+        ("indices", C.c_void_p),
+        ("indptr", C.c_void_p),
+        ("index_type", C.c_int),
+        ("nnz", C.c_uint64),
+        ("num_major", C.c_uint64),
+        ("is_csr", C.c_int),
+        ("num_genes", C.c_uint32),
+        ("cell_indices", C.c_void_p),
+        ("num_cell_indices", C.c_uint64),
+        ("cell_mask", C.c_void_p),
+        ("cell_mask_len", C.c_uint64),
+        ("on_device", C.c_int),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/briscgpu.h declares
 _vp, _u32, _u64, _i, _f = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
 SIGNATURES = {
@@ -106,6 +126,8 @@ SIGNATURES = {
     "bgpu_size_factors": (_i, [_vp, _i, _vp, _i, _u64, _i, _vp, _vp, _vp, _vp, _vp]),
     "bgpu_normalize_csr": (_i, [_vp, _i, _vp, _i, _u64, _vp, _vp, _vp, _vp]),
     "bgpu_csr_tocsc": (_i, [_u64, _u32, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    "bgpu_gene_mean_var": (_i, [C.POINTER(HvgInput), _u64, _vp, _vp, _vp, _vp]),
+    "bgpu_clipped_sum": (_i, [C.POINTER(HvgInput), _u64, _vp, _vp, _vp, _vp]),
 }
 
 _lock = threading.Lock()

@@ -54,7 +54,11 @@ enum {
   BGPU_VALUE_U16 = 0,  /* raw counts, uint16                                   */
   BGPU_VALUE_U32 = 1,  /* raw counts, uint32 (must be <= 65535)                */
   BGPU_VALUE_I32 = 2,  /* raw counts, int32  (must be in [0, 65535])           */
-  BGPU_VALUE_F32 = 3   /* float32: already-normalised values, or float counts  */
+  BGPU_VALUE_F32 = 3,  /* float32: already-normalised values, or float counts  */
+  /* the HVG statistics below also take the reference's other `numeric` types */
+  BGPU_VALUE_I64 = 4,  /* int64 counts                                          */
+  BGPU_VALUE_U64 = 5,  /* uint64 counts                                         */
+  BGPU_VALUE_F64 = 6   /* float64 counts                                        */
 };
 
 /* Normalisation applied to the stored values (brisc/normalize.pyx method_number).
@@ -269,6 +273,47 @@ BGPU_API int bgpu_normalize_csr(const void* indptr, int index_type, const void* 
 BGPU_API int bgpu_csr_tocsc(uint64_t n_row, uint32_t n_col, const void* Ap,
                    const void* Aj, const void* Ax, int index_type, void* Bp,
                    void* Bi, void* Bx, void* stream);
+
+/* ---- highly-variable-gene statistics (brisc/hvg.pyx) -------------------- */
+/* A raw count matrix in CSR (cells x genes) or CSC (genes x cells), with the
+ * subset of cells the reference's functions take. The counts are cast to
+ * uint64 as the reference casts them (values must be non-negative) and summed
+ * exactly; the results are bit-identical to the reference's. */
+typedef struct bgpu_hvg_input {
+  const void* data;          /* nnz values, value_type (any BGPU_VALUE_*)       */
+  int value_type;
+  const void* indices;       /* nnz gene (CSR) or cell (CSC) indices            */
+  const void* indptr;        /* num_major + 1 offsets                           */
+  int index_type;            /* BGPU_INDEX_*                                    */
+  uint64_t nnz;
+  uint64_t num_major;        /* rows (CSR) or genes (CSC) of indptr             */
+  int is_csr;
+  uint32_t num_genes;        /* num_dataset_genes (CSR; for CSC mean/variance
+                                the leading genes of indptr)                   */
+  const int64_t* cell_indices; /* CSR subset (may be NULL)                      */
+  uint64_t num_cell_indices;
+  const int8_t* cell_mask;   /* CSC subset, one byte per cell (may be NULL)     */
+  uint64_t cell_mask_len;
+  int on_device;             /* 1: every array here and every output is a
+                                device pointer; 0: host arrays                 */
+} bgpu_hvg_input;
+
+/* Per-gene mean, sample variance and nonzero count (float, float, uint32;
+ * num_genes each). Replaces gene_mean_and_variance_csr (brisc/hvg.pyx:9-139:
+ * without cell_indices every stored entry counts, with it the first
+ * num_cells listed cells) and gene_mean_and_variance_csc (hvg.pyx:142-252,
+ * cells where cell_mask is nonzero). num_cells divides as in the reference. */
+BGPU_API int bgpu_gene_mean_var(const bgpu_hvg_input* in, uint64_t num_cells,
+                                float* mean, float* var, uint32_t* nonzero_count,
+                                void* stream);
+/* Per-gene sums and squared sums of counts, each count above clip_val[gene]
+ * replaced by clip_val[gene]. Replaces clipped_sum_csr (hvg.pyx:255-403:
+ * rows [0, num_cells), or every listed cell) and clipped_sum_csc
+ * (hvg.pyx:406-530: every gene of indptr, num_cells unused). Outputs have
+ * num_genes (CSR) or num_major (CSC) entries. */
+BGPU_API int bgpu_clipped_sum(const bgpu_hvg_input* in, uint64_t num_cells,
+                              const float* clip_val, float* batch_counts_sum,
+                              float* squared_batch_counts_sum, void* stream);
 
 #ifdef __cplusplus
 }

@@ -6,7 +6,7 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 
 1. ``cythonize`` (needs Cython and the reference checkout): translate the
    reference modules on the path -- ``brisc/cyutils.pyx``, ``brisc/pca.pyx``,
-   ``brisc/normalize.pyx``, ``brisc/cysparse.pyx`` -- plus the test harness
+   ``brisc/normalize.pyx``, ``brisc/cysparse.pyx``, ``brisc/hvg.pyx`` -- plus the test harness
    ``oracle/ref_probe.pyx`` to C++ under ``oracle/_ref/gen/``. The sources are
    read where they lie; nothing is copied into the repository.
 2. ``compile`` (needs only g++, Python and numpy headers): build every
@@ -37,10 +37,10 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 GEN = REF_OUT / "gen"
-MODULES = ["cyutils", "pca", "normalize", "cysparse"]
-# What the CPU baseline needs (cysparse's 24 MB of C++ is only needed for the
+MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg"]
+# What the CPU baselines need (cysparse's 24 MB of C++ is only needed for the
 # transpose fixture and is skipped where compile time matters).
-BASELINE_MODULES = ["cyutils", "pca", "normalize", "ref_probe"]
+BASELINE_MODULES = ["cyutils", "pca", "normalize", "hvg", "ref_probe"]
 DIRECTIVES = {"language_level": "3", "boundscheck": False,
               "wraparound": False, "cdivision": True,
               "initializedcheck": False, "warn.undeclared": False}

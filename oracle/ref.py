@@ -1,6 +1,6 @@
 """ORACLE (test/baseline infrastructure): the reference's own compiled modules.
 
-``load()`` imports brisc's ``pca``, ``normalize``, ``cysparse`` and the
+``load()`` imports brisc's ``pca``, ``normalize``, ``cysparse``, ``hvg`` and the
 ``ref_probe`` harness from ``oracle/_ref/<machine>/`` (built by
 oracle/build_ref.py from the reference checkout, or from the generated C++
 that travels with the repository when no checkout is present). Returns None
@@ -58,11 +58,11 @@ def load(build: bool = True):
     if str(d) not in sys.path:
         sys.path.insert(0, str(d))
     _mods = {}
-    for name in ("cyutils", "pca", "normalize", "cysparse", "ref_probe"):
+    for name in ("cyutils", "pca", "normalize", "cysparse", "hvg", "ref_probe"):
         try:
             _mods[name] = importlib.import_module(f"brisc.{name}")
         except ImportError:
-            if name != "cysparse":
+            if name not in ("cysparse", "hvg"):
                 raise
     return _mods
 

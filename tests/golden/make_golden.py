@@ -12,8 +12,13 @@ reference's outputs, so the tests never regenerate data:
 * tocsc.npz      csr_tocsc (brisc/cysparse.pyx:1179) of the same matrix.
 * irlba.npz      irlba PCs (brisc/pca.pyx:661) on clustered NB matrices whose
                  top singular values are separated, plus one flat-spectrum case.
+* hvg.npz        gene_mean_and_variance_csr/_csc and clipped_sum_csr/_csc
+                 (brisc/hvg.pyx) on an NB count matrix with a few large
+                 counts, over all cells and over a cell subset, uint32 and
+                 float32 counts, int32 and int64 indices.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py hvg      # hvg.npz only
 """
 from __future__ import annotations
 
@@ -32,11 +37,60 @@ OUT = Path(__file__).resolve().parent
 SEEDS = [0, 1, 7, 42, 12345, 2**63 + 5]
 
 
+def make_hvg(M) -> None:
+    import scipy.sparse as sp
+    H = M["hvg"]
+    C = nb_counts(900, 160, seed=23, density=0.1, workers=1)
+    A = sp.csr_matrix((C.data.astype(np.uint32), C.indices, C.indptr),
+                      shape=(C.num_cells, C.num_genes))
+    big = np.random.default_rng(5).random(A.nnz) < 0.003  # counts above 2^16
+    A.data[big] = A.data[big] * 4099 + 70000
+    B = A.tocsc()
+    B.sort_indices()
+    n, g = A.shape
+    cells = np.arange(0, n, 3, dtype=np.int64)
+    mask = np.zeros(n, np.int8)
+    mask[cells] = 1
+    clip = (np.random.default_rng(6).random(g) * 12 + 0.5).astype(np.float32)
+    out = {"n": np.int64(n), "g": np.int64(g), "csr_data": A.data, "csr_indices": A.indices,
+           "csr_indptr": A.indptr, "csc_data": B.data, "csc_indices": B.indices,
+           "csc_indptr": B.indptr, "cells": cells, "mask": mask, "clip": clip}
+    for dt in (np.uint32, np.float32):
+        for it in (np.int32, np.int64):
+            tag = f"{np.dtype(dt).name}_{np.dtype(it).name}"
+            ad, ai, ap = A.data.astype(dt), A.indices.astype(it), A.indptr.astype(it)
+            bd, bi, bp = B.data.astype(dt), B.indices.astype(it), B.indptr.astype(it)
+            for sub in ("all", "sub"):
+                c = cells if sub == "sub" else np.zeros(0, np.int64)
+                mk = mask if sub == "sub" else np.zeros(0, np.int8)
+                nc = len(cells) if sub == "sub" else n
+                for form in ("csr", "csc"):
+                    m_, v_, z_ = (np.zeros(g, np.float32), np.zeros(g, np.float32),
+                                  np.zeros(g, np.uint32))
+                    if form == "csr":
+                        H.gene_mean_and_variance_csr(ad, ai, ap, c, nc, g, m_, v_, z_, 4)
+                    else:
+                        H.gene_mean_and_variance_csc(bd, bi, bp, mk, nc, g, m_, v_, z_, 4)
+                    b_, q_ = np.zeros(g, np.float32), np.zeros(g, np.float32)
+                    if form == "csr":
+                        H.clipped_sum_csr(ad, ai, ap, nc, g, c, clip, b_, q_, 4)
+                    else:
+                        H.clipped_sum_csc(bd, bi, bp, mk, clip, b_, q_, 4)
+                    key = f"{form}_{tag}_{sub}"
+                    out.update({f"{key}_mean": m_, f"{key}_var": v_, f"{key}_nnz": z_,
+                                f"{key}_bsum": b_, f"{key}_bsq": q_})
+    np.savez_compressed(OUT / "hvg.npz", **out)
+
+
 def main() -> int:
     M = ref.load()
     if M is None:
         print("reference modules unavailable", file=sys.stderr)
         return 1
+    if "hvg" in M:
+        make_hvg(M)
+    if sys.argv[1:] == ["hvg"]:
+        return 0
     probe = M["ref_probe"]
 
     rng = {}

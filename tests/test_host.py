@@ -82,3 +82,26 @@ def test_reorth_modes():
     for bad in (0, 3, "two", None, 1.5):
         with pytest.raises(ValueError, match="reorth_passes"):
             reorth_code(bad)
+
+
+def test_hvg_argument_checks():
+    """Type and shape checks of the HVG entry points run before any GPU call."""
+    from brisc_gb300 import hvg
+    ip = np.array([0, 1, 2], np.int32)
+    ix = np.array([0, 1], np.int32)
+    d = np.array([1, 2], np.uint32)
+    m, v, c = np.zeros(2, np.float32), np.zeros(2, np.float32), np.zeros(2, np.uint32)
+    with pytest.raises(TypeError, match="same dtype"):
+        hvg.gene_mean_and_variance_csr(d, ix.astype(np.int64), ip, np.zeros(0, np.int64),
+                                       2, 2, m, v, c, 1)
+    with pytest.raises(TypeError, match="data has dtype int8"):
+        hvg.gene_mean_and_variance_csr(d.astype(np.int8), ix, ip, np.zeros(0, np.int64),
+                                       2, 2, m, v, c, 1)
+    with pytest.raises(ValueError, match="entries"):
+        hvg.gene_mean_and_variance_csr(d, ix, ip, np.zeros(0, np.int64), 2, 3, m, v, c, 1)
+    with pytest.raises(TypeError, match="cell_indices"):
+        hvg.clipped_sum_csr(d, ix, ip, 2, 2, np.array([0], np.int32),
+                            np.ones(2, np.float32), m, v, 1)
+    with pytest.raises(ValueError, match="C-contiguous"):
+        hvg.clipped_sum_csc(d, ix, ip, np.zeros(0, np.int8),
+                            np.ones(4, np.float32)[::2], m, v, 1)

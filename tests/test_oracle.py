@@ -115,3 +115,51 @@ def test_flat_spectrum_singular_values(golden):
     o = oirlba.irlba(X, k, m, reorth_passes=2)
     assert dense.rel_sv_error(z["flat_pcs"], S).max() < 1e-4
     assert dense.rel_sv_error(o["PCs"], S).max() < 1e-4
+
+
+HVG_TAGS = ["uint32_int32", "uint32_int64", "float32_int32", "float32_int64"]
+
+
+def hvg_case(z, form, tag):
+    """(data, indices, indptr) of the hvg fixture in one dtype combination."""
+    dt, it = (np.dtype(t) for t in tag.split("_"))
+    return (z[f"{form}_data"].astype(dt), z[f"{form}_indices"].astype(it),
+            z[f"{form}_indptr"].astype(it))
+
+
+@pytest.mark.parametrize("sub", ["all", "sub"])
+@pytest.mark.parametrize("form", ["csr", "csc"])
+@pytest.mark.parametrize("tag", HVG_TAGS)
+def test_hvg_oracle_bit_exact(golden, tag, form, sub):
+    """The HVG restatement against the reference's own outputs
+    (brisc/hvg.pyx), integer and float results alike, bit for bit."""
+    from oracle import hvg as oh
+    z = golden("hvg")
+    n, g = int(z["n"]), int(z["g"])
+    d, ix, ip = hvg_case(z, form, tag)
+    cells = z["cells"] if sub == "sub" else np.zeros(0, np.int64)
+    mask = z["mask"] if sub == "sub" else np.zeros(0, np.int8)
+    nc = len(cells) if sub == "sub" else n
+    key = f"{form}_{tag}_{sub}"
+    if form == "csr":
+        m, v, c = oh.gene_mean_and_variance_csr(d, ix, ip, cells, nc, g)
+        b, q = oh.clipped_sum_csr(d, ix, ip, nc, g, cells, z["clip"])
+    else:
+        m, v, c = oh.gene_mean_and_variance_csc(d, ix, ip, mask, nc, g)
+        b, q = oh.clipped_sum_csc(d, ix, ip, mask, z["clip"])
+    for got, name in ((m, "mean"), (v, "var"), (c, "nnz"), (b, "bsum"), (q, "bsq")):
+        assert np.array_equal(got, z[f"{key}_{name}"]), name
+
+
+def test_hvg_oracle_fma_forms():
+    """The clipped sums are fused multiply-adds in the reference's build (the
+    fixture above pins that); the restatement's fma rounds once: for
+    a = b = 1 + 2^-12, c = -1 it keeps the 2^-24 term that two roundings
+    lose."""
+    from oracle import hvg as oh
+    a = np.float32(1 + 2.0 ** -12)
+    one = np.float32(-1)
+    assert oh.fma_f32(a, a, one) == np.float32(2.0 ** -11 + 2.0 ** -24)
+    assert np.float32(np.float32(a * a) + one) == np.float32(2.0 ** -11)
+    assert oh.fma_f32(np.float32(0), np.float32(5), np.float32(-2.5)) == np.float32(-2.5)
+    assert oh.fma_f32(np.float32(3e38), np.float32(10), np.float32(0)) == np.float32(np.inf)
