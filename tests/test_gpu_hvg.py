@@ -129,3 +129,39 @@ def test_hvg_out_of_range_index_rejected(cuda):
     with pytest.raises(ValueError, match="out of bounds"):
         hvg.gene_mean_and_variance_csc(d, np.array([0, 1, 0], np.int32), ip, mask, 2, 2,
                                        m, v, c, 1)
+
+
+def test_hvg_called_as_single_cell_calls_it(cuda, golden):
+    """The keyword calls of SingleCell's HVG step (brisc/single_cell.py:
+    11320-11395): CSR with an int64 cell list and num_cells = its length,
+    CSC with a boolean cell mask."""
+    z = golden("hvg")
+    n, g = int(z["n"]), int(z["g"])
+    cells = z["cells"]
+    for form in ("csr", "csc"):
+        d, ix, ip = hvg_case(z, form, "float32_int32")
+        mean, var = np.zeros(g, np.float32), np.zeros(g, np.float32)
+        nz = np.zeros(g, np.uint32)
+        b, q = np.empty(g, np.float32), np.empty(g, np.float32)
+        if form == "csr":
+            hvg.gene_mean_and_variance_csr(
+                data=d, indices=ix, indptr=ip, cell_indices=cells,
+                num_cells=len(cells), num_dataset_genes=g, mean=mean, var=var,
+                nonzero_count=nz, num_threads=4)
+            hvg.clipped_sum_csr(
+                data=d, indices=ix, indptr=ip, num_cells=len(cells),
+                num_dataset_genes=g, cell_indices=cells, clip_val=z["clip"],
+                batch_counts_sum=b, squared_batch_counts_sum=q, num_threads=4)
+        else:
+            mask = z["mask"].astype(bool)
+            hvg.gene_mean_and_variance_csc(
+                data=d, indices=ix, indptr=ip, cell_mask=mask,
+                num_cells=int(mask.sum()), num_dataset_genes=g, mean=mean, var=var,
+                nonzero_count=nz, num_threads=4)
+            hvg.clipped_sum_csc(
+                data=d, indices=ix, indptr=ip, cell_mask=mask, clip_val=z["clip"],
+                batch_counts_sum=b, squared_batch_counts_sum=q, num_threads=4)
+        key = f"{form}_float32_int32_sub"
+        for a, name in ((mean, "mean"), (var, "var"), (nz, "nnz"), (b, "bsum"),
+                        (q, "bsq")):
+            assert np.array_equal(a, z[f"{key}_{name}"]), (form, name)
