@@ -1,7 +1,8 @@
 // Dense kernels of the IRLBA solve: the fused U pass of brisc/pca.pyx:997-1090
-// split into fixed-block dot / update kernels (classical Gram-Schmidt, run
-// once as the reference or twice for CGS2), the V-side step of pca.pyx:1103-1171
-// and the tall-skinny rotations of pca.pyx:1210-1255.
+// split into fixed-block dot / update kernels (classical Gram-Schmidt: once as
+// the reference, a second time only where the first cancels, or always twice
+// for CGS2), the V-side step of pca.pyx:1103-1171 and the tall-skinny
+// rotations of pca.pyx:1210-1255.
 //
 // Determinism: every sum is either a per-thread sequence in a fixed order, a
 // fixed xor-shuffle tree, or a sum over fixed 1024-row blocks in block order.

@@ -224,8 +224,9 @@ def test_cancel_flag(cuda, golden):
 
 def test_large_solve_meets_fp64_gate(cuda):
     """200k cells x 2000 genes at 5% density (the 1M workload's generator),
-    default settings (FP32 small SVD with the FP64 polish, CGS2, tensor-core
-    rotation): relative singular-value error <= 1e-4 against the FP64
+    default settings (FP32 small SVD with the FP64 polish, adaptive
+    Gram-Schmidt, tensor-core rotation): relative singular-value error <= 1e-4
+    against the FP64
     Gram-matrix oracle, and the solve converges."""
     from brisc_gb300.synth import nb_counts
     c = nb_counts(200_000, 2000, seed=0, density=0.05)
