@@ -163,3 +163,20 @@ def test_hvg_oracle_fma_forms():
     assert np.float32(np.float32(a * a) + one) == np.float32(2.0 ** -11)
     assert oh.fma_f32(np.float32(0), np.float32(5), np.float32(-2.5)) == np.float32(-2.5)
     assert oh.fma_f32(np.float32(3e38), np.float32(10), np.float32(0)) == np.float32(np.inf)
+
+
+def test_oracle_adaptive_mode_second_passes_where_needed():
+    """The adaptive restatement (reorth_passes=0) takes a second pass only
+    where the first cancels: none on an NB fixture, some on a near-low-rank
+    matrix, and both meet the FP64 singular-value gate."""
+    rng = np.random.default_rng(0)
+    n, g, r = 4000, 400, 8
+    W = rng.random((n, r)) * (rng.random((n, r)) < 0.3)
+    H = rng.random((r, g)) * (rng.random((r, g)) < 0.5)
+    A = W @ H
+    A = A + 1e-3 * rng.random((n, g)) * (A > 0)
+    X = sp.csr_matrix(A.astype(np.float32))
+    o = oirlba.irlba(X, 6, 16, reorth_passes=0)
+    assert 0 < o["second_passes"] < o["steps"] - 1
+    S, U, Vt = dense.top_svd(X.astype(np.float64), 8)
+    assert dense.rel_sv_error(o["PCs"], S).max() < 1e-4
