@@ -165,10 +165,16 @@ def test_hvg_oracle_fma_forms():
     assert oh.fma_f32(np.float32(3e38), np.float32(10), np.float32(0)) == np.float32(np.inf)
 
 
-def test_oracle_adaptive_mode_second_passes_where_needed():
+def test_oracle_adaptive_mode_second_passes_where_needed(golden):
     """The adaptive restatement (reorth_passes=0) takes a second pass only
     where the first cancels: none on an NB fixture, some on a near-low-rank
     matrix, and both meet the FP64 singular-value gate."""
+    z = golden("irlba")
+    Xb, kb, mb = _case(z, "clustered_b")
+    ob = oirlba.irlba(Xb, kb, mb, reorth_passes=0)
+    assert ob["second_passes"] == 0 and ob["second_passes_v"] == 0
+    Sb, _, _ = dense.top_svd(Xb, kb + 2)
+    assert dense.rel_sv_error(ob["PCs"], Sb).max() < 1e-4
     rng = np.random.default_rng(0)
     n, g, r = 4000, 400, 8
     W = rng.random((n, r)) * (rng.random((n, r)) < 0.3)
