@@ -174,3 +174,22 @@ def clipped_sum_csc(data, indices, indptr, cell_mask, clip_val, batch_counts_sum
     h = _input(data, indices, indptr, False, _len(indptr) - 1, cell_mask=cell_mask)
     _clipped(h, 0, _len(indptr) - 1, clip_val, batch_counts_sum,
              squared_batch_counts_sum, data)
+
+
+NAMES = ("gene_mean_and_variance_csr", "gene_mean_and_variance_csc",
+         "clipped_sum_csr", "clipped_sum_csc")
+
+
+def install_hvg(module=None) -> dict:
+    """Bind the four functions into brisc's ``single_cell`` module, where
+    ``import_cython`` puts the reference's (brisc/single_cell.py:34-43) and
+    its HVG step calls them (single_cell.py:11330-11391). Returns the
+    previous bindings, for restoring with ``install_hvg`` of a module whose
+    attributes are those values, or by hand."""
+    if module is None:
+        import brisc.single_cell as module  # pragma: no cover
+    previous = {name: getattr(module, name, None) for name in NAMES}
+    here = globals()
+    for name in NAMES:
+        setattr(module, name, here[name])
+    return previous

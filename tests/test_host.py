@@ -105,3 +105,14 @@ def test_hvg_argument_checks():
     with pytest.raises(ValueError, match="C-contiguous"):
         hvg.clipped_sum_csc(d, ix, ip, np.zeros(0, np.int8),
                             np.ones(4, np.float32)[::2], m, v, 1)
+
+
+def test_install_hvg_binds_and_returns_previous():
+    import types
+    from brisc_gb300 import hvg
+    fake = types.SimpleNamespace(gene_mean_and_variance_csr="old")
+    prev = hvg.install_hvg(fake)
+    assert prev["gene_mean_and_variance_csr"] == "old"
+    assert prev["clipped_sum_csc"] is None
+    for name in hvg.NAMES:
+        assert getattr(fake, name) is getattr(hvg, name)
