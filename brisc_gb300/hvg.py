@@ -184,8 +184,7 @@ def install_hvg(module=None) -> dict:
     """Bind the four functions into brisc's ``single_cell`` module, where
     ``import_cython`` puts the reference's (brisc/single_cell.py:34-43) and
     its HVG step calls them (single_cell.py:11330-11391). Returns the
-    previous bindings, for restoring with ``install_hvg`` of a module whose
-    attributes are those values, or by hand."""
+    previous bindings (name -> function), for restoring them."""
     if module is None:
         import brisc.single_cell as module  # pragma: no cover
     previous = {name: getattr(module, name, None) for name in NAMES}
