@@ -81,3 +81,37 @@ def test_invalid_arguments_rejected_without_gpu(built_lib):
     assert L.bgpu_matrix_create(C.byref(h), C.byref(d), None) == _lib.ERR_INVALID
     with pytest.raises(ValueError):
         _lib.call("bgpu_start_vector", 0, 0, None)
+
+
+def test_hvg_arguments_rejected_without_gpu(built_lib):
+    """bgpu_gene_mean_var validates its input description before any CUDA
+    call: unknown element types and a subset of the wrong kind."""
+    import numpy as np
+    from brisc_gb300 import _lib
+    L = _lib.lib()
+    ip = np.array([0, 1], np.int32)
+    ix = np.array([0], np.int32)
+    d = np.array([1], np.uint32)
+    out = np.zeros(1, np.float32)
+    nz = np.zeros(1, np.uint32)
+
+    def run(**kw):
+        h = _lib.HvgInput()
+        h.data, h.value_type = d.ctypes.data, _lib.VALUE_U32
+        h.indices, h.indptr, h.index_type = ix.ctypes.data, ip.ctypes.data, _lib.INDEX_I32
+        h.nnz, h.num_major, h.is_csr, h.num_genes = 1, 1, 1, 1
+        for k, v in kw.items():
+            setattr(h, k, v)
+        return L.bgpu_gene_mean_var(C.byref(h), 1, out.ctypes.data, out.ctypes.data,
+                                    nz.ctypes.data, None)
+
+    assert run(value_type=99) == _lib.ERR_INVALID
+    assert b"value_type" in L.bgpu_last_error()
+    assert run(index_type=7) == _lib.ERR_INVALID
+    assert b"index_type" in L.bgpu_last_error()
+    mask = np.ones(1, np.int8)
+    assert run(cell_mask=mask.ctypes.data, cell_mask_len=1) == _lib.ERR_INVALID
+    assert b"cell_mask" in L.bgpu_last_error()
+    assert run(is_csr=0, num_genes=5) == _lib.ERR_INVALID
+    assert b"fewer genes" in L.bgpu_last_error()
+    assert L.bgpu_gene_mean_var(None, 1, None, None, None, None) == _lib.ERR_INVALID
