@@ -66,9 +66,7 @@ def build(jobs: int | None = None, verbose: bool = False,
     with ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(one, srcs))
     if not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
-        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs),
-               "-lcuda"] if False else [cc, *ARCH, "-shared", "-o", str(LIB),
-                                         *map(str, objs)]
+        cmd = [cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -12,8 +12,9 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 2. ``compile`` (needs only g++, Python and numpy headers): build every
    ``oracle/_ref/gen/*.cpp`` into ``oracle/_ref/<machine>/brisc/*.so`` with the
    reference's own Linux flags (``setup.py:92-100`` of the reference:
-   ``-Ofast -funroll-loops -std=c++17 -fopenmp`` plus the baseline ``-march``
-   variant of the machine, ``setup.py:38-45``).
+   ``-Ofast -funroll-loops -std=c++17 -fopenmp`` plus the ``-march`` of the
+   variant the reference would load on this CPU, ``setup.py:34-42`` and
+   ``brisc/utils.py:29-49``: the SVE build on Grace).
 
 Stage 2 runs on any machine that received ``oracle/_ref/gen`` (the C++ is
 architecture-neutral), so the aarch64 GPU host can rebuild the reference
@@ -46,16 +47,36 @@ DIRECTIVES = {"language_level": "3", "boundscheck": False,
               "initializedcheck": False, "warn.undeclared": False}
 
 
+def reference_dir() -> Path:
+    """The reference checkout this recipe reads: $BRISC_REFERENCE, else the
+    container's read-only mount. Absent on machines that only compile."""
+    return Path(os.environ.get("BRISC_REFERENCE", "/root/reference"))
+
+
+def have_reference() -> bool:
+    return (reference_dir() / "brisc" / "pca.pyx").exists()
+
+
 def machine_dir() -> Path:
     return REF_OUT / platform.machine().lower()
 
 
 def march_flag() -> list[str]:
+    """The -march of the variant the reference itself would load here: its
+    setup.py:34-42 builds one per instruction-set level and its
+    import_cython (brisc/utils.py:29-49) picks x86-64-v4 with AVX-512F, v3
+    with AVX2, else v2; on aarch64 the SVE build where the CPU has SVE (as
+    Grace does), else plain armv8.2-a."""
     m = platform.machine().lower()
+    try:
+        from numpy._core._multiarray_umath import __cpu_features__ as cpu
+    except ImportError:
+        cpu = {}
     if m in ("x86_64", "amd64"):
-        return ["-march=x86-64-v3"]
+        return ["-march=x86-64-v4" if cpu.get("AVX512F") else
+                "-march=x86-64-v3" if cpu.get("AVX2") else "-march=x86-64-v2"]
     if m == "aarch64":
-        return ["-march=armv8.2-a"]
+        return ["-march=armv8.2-a+sve" if cpu.get("SVE") else "-march=armv8.2-a"]
     return []
 
 
@@ -100,10 +121,14 @@ def compile_all(jobs: int, modules: list[str] | None = None) -> Path:
             f"no generated C++ under {GEN}; run the cythonize stage where "
             "the reference checkout and Cython are available")
 
+    # the flags of the last build: a different -march rebuilds everything
+    stamp = machine_dir() / "flags.txt"
+    same_flags = stamp.exists() and stamp.read_text() == " ".join(flags)
+
     def one(cpp: Path) -> str:
         mod = cpp.stem.split(".", 1)[1]
         so = out_pkg / f"{mod}{ext}"
-        if so.exists() and so.stat().st_mtime >= cpp.stat().st_mtime:
+        if same_flags and so.exists() and so.stat().st_mtime >= cpp.stat().st_mtime:
             return f"up to date {so.name}"
         cmd = ["g++", *flags, str(cpp), "-o", str(so), "-fopenmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -114,12 +139,22 @@ def compile_all(jobs: int, modules: list[str] | None = None) -> Path:
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         for msg in ex.map(one, cpps):
             print(msg)
+    stamp.write_text(" ".join(flags))
     return machine_dir()
+
+
+def built_march() -> str:
+    """The -march the compiled reference modules here were built with."""
+    stamp = machine_dir() / "flags.txt"
+    if not stamp.exists():
+        return "unknown"
+    return next((f for f in stamp.read_text().split() if f.startswith("-march")),
+                "default")
 
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=str(reference_dir()))
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--compile-only", action="store_true")
     ap.add_argument("--baseline-only", action="store_true",

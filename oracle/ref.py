@@ -43,10 +43,9 @@ def load(build: bool = True):
     have = pkg.exists() and any(pkg.glob("pca*.so"))
     if not have and build:
         from . import build_ref
-        ref = Path("/root/reference")
         try:
-            if (ref / "brisc" / "pca.pyx").exists():
-                build_ref.cythonize(ref)
+            if build_ref.have_reference():
+                build_ref.cythonize(build_ref.reference_dir())
             build_ref.compile_all(os.cpu_count() or 4,
                                   modules=build_ref.BASELINE_MODULES)
         except Exception as e:  # noqa: BLE001 - reported to the caller
@@ -123,8 +122,16 @@ def run_irlba(indptr, indices, data_f32, n: int, g: int, k: int = 50,
     serial = num_threads == 1 and not match_parallel
     if serial:
         csc = (indptr, indices, data_f32)
-    elif csc is None:
+    elif csc is None and "cysparse" in M:
         csc = tocsc(indptr, indices, data_f32, n, g, num_threads)
+    elif csc is None:
+        # cysparse is left out of the baseline build (24 MB of C++): scipy's
+        # transpose keeps rows ascending inside each column, as csr_tocsc
+        # does (brisc/cysparse.pyx:1179-1295), so the arrays are the same
+        import scipy.sparse as sp
+        t = sp.csr_matrix((data_f32, indices, indptr), shape=(n, g)).tocsc()
+        t.sort_indices()
+        csc = (t.indptr.astype(indptr.dtype), t.indices.astype(indices.dtype), t.data)
     PCs = np.zeros((n, k), dtype=np.float32)
     with _blas1():
         conv = M["pca"].irlba(

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import hashlib
 import os
+import tempfile
 from concurrent.futures import ProcessPoolExecutor
 from dataclasses import dataclass
 from multiprocessing import get_context
@@ -149,8 +150,8 @@ def cached_nb_counts(num_cells: int, num_genes: int = 2000, seed: int = 0,
     processes benchmarking the same workload generate it once."""
     key = repr((num_cells, num_genes, seed, sorted(kw.items())))
     h = hashlib.sha1(key.encode()).hexdigest()[:16]
-    d = Path(cache_dir or os.environ.get("BRISC_GB300_CACHE",
-                                         "/tmp/brisc_gb300_cache"))
+    d = Path(cache_dir or os.environ.get("BRISC_GB300_CACHE")
+             or Path(tempfile.gettempdir()) / "brisc_gb300_cache")
     f = d / f"nb_{num_cells}x{num_genes}_s{seed}_{h}.npz"
     if f.exists():
         z = np.load(f)

@@ -10,7 +10,7 @@ import scipy.sparse as sp
 
 from brisc_gb300 import DeviceMatrix
 from brisc_gb300.batch import SharedMatrix, pca_subsets, subset_solve_params
-from brisc_gb300.synth import nb_counts
+from synth import nb_counts
 from oracle import dense
 
 pytestmark = pytest.mark.gpu

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from brisc_gb300.serve import PCARequest, PCAServer, gpu_solve
-from brisc_gb300.synth import nb_counts
+from synth import nb_counts
 
 pytestmark = pytest.mark.gpu
 

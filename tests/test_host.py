@@ -8,7 +8,7 @@ import pytest
 import scipy.sparse as sp
 
 from brisc_gb300 import pca
-from brisc_gb300.synth import nb_counts
+from synth import nb_counts
 
 
 def _X(n=50, g=20, dtype=np.float32):
