@@ -110,6 +110,7 @@ SIGNATURES = {
     "bgpu_matrix_create_rows": (_i, [C.POINTER(_vp), C.POINTER(MatrixDesc), _vp, _u64, _vp]),
     "bgpu_matrix_destroy": (_i, [_vp]),
     "bgpu_matrix_bytes": (_i, [_vp, C.POINTER(_u64)]),
+    "bgpu_matrix_layout": (_i, [_vp, C.POINTER(C.c_int)]),
     "bgpu_matrix_matvec": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "bgpu_matrix_rmatvec": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "bgpu_matrix_gene_stddev": (_i, [_vp, _vp, _vp]),

@@ -162,7 +162,7 @@ struct Solver {
   float tol;
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
-      Vbt, Ub2, Vbt2, gram, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
+      Vbt, oaw, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
       sb64, ratios,
       derr, taken, ticket;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
@@ -253,9 +253,7 @@ struct Solver {
     BGPU_TRY(balloc(Ub, (size_t)m * m * 4, true, s));
     BGPU_TRY(balloc(Sb, (size_t)m * 4, true, s));
     BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
-    BGPU_TRY(balloc(Ub2, (size_t)m * m * 4, true, s));
-    BGPU_TRY(balloc(Vbt2, (size_t)m * (m + 1) * 4, true, s));
-    BGPU_TRY(balloc(gram, (size_t)m * m * 8, true, s));
+    BGPU_TRY(balloc(oaw, svd_refine_doubles(m) * 8, true, s));
     if (jacobi_smem_bytes(m, svd64) > 220 * 1024)
       BGPU_TRY(balloc(svdwork, jacobi_global_bytes(m, svd64), true, s));
     BGPU_TRY(balloc(ub_last, (size_t)m * 8, true, s));
@@ -283,7 +281,9 @@ struct Solver {
     float* coef2 = coefp + ps;
     float* Up = U.as<float>();
     BGPU_TRY(ev_begin(0));
-    if (X.stream_ok && X.impl == 0)
+    if (X.sell)
+      BGPU_TRY(launch_xv_sell(X, Vcol(j), sd.as<float>(), y0p, s));
+    else if (X.stream_ok && X.impl == 0)
       BGPU_TRY(launch_matvec_stream(X, Vcol(j), sd.as<float>(), y0p,
                                     derr.as<int>(), s));
     else
@@ -363,7 +363,9 @@ struct Solver {
     }
     BGPU_TRY(ev_end());
     BGPU_TRY(ev_begin(1));
-    if (X.stream_ok && X.impl == 0)
+    if (X.sell)
+      BGPU_TRY(launch_xt_sell(X, yfin, scalp + 1, Ucol(j), zpart.as<float>(), s));
+    else if (X.stream_ok && X.impl == 0)
       BGPU_TRY(launch_rmatvec_stream(X, yfin, scalp + 1, Ucol(j),
                                      zpart.as<float>(), derr.as<int>(), s));
     else
@@ -384,6 +386,8 @@ struct Solver {
 };
 
 }  // namespace
+
+constexpr int kRefineSteps = 3;  // Newton steps after the FP32 Jacobi
 
 int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
                 int pcs_on_device, float* svals, float* loadings,
@@ -409,9 +413,8 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
   {
     S.svd64 = o.svd_fp64 != 0;
     BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
-    const bool tc_ok = gemm_tc_supported(o.subspace_size, o.subspace_size);
-    BGPU_REQUIRE(o.rotation_mode != 2 || tc_ok, BGPU_ERR_UNSUPPORTED,
-                 "tensor-core rotation needs subspace_size <= 104");
+    // subspaces beyond one shared-memory staging run as K / column chunks
+    const bool tc_ok = o.subspace_size <= 1024;
     S.rot_mode = o.rotation_mode == 0 ? (tc_ok ? 2 : 1) : (int)o.rotation_mode;
     const char* et = std::getenv("BGPU_TRACE");
     S.trace = et && et[0] == '1';
@@ -457,21 +460,19 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
       BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), nullptr, m, S.Ub.as<float>(),
                                  S.Sb.as<float>(), S.Vbt.as<float>(), nullptr,
                                  nullptr, S.svdwork.p, S.svdinfo.as<int>(), s));
-      // FP64-accumulated polish of the FP32 factors: Ub's columns and Vbt's
-      // rows back to orthonormal before they rotate the bases
-      BGPU_TRY(launch_orthonormalize(S.Ub.as<float>(), m, m, m, 1, S.gram.as<double>(),
-                                     S.Ub2.as<float>(), s));
-      BGPU_TRY(launch_orthonormalize(S.Vbt.as<float>(), m, m + 1, 1, m,
-                                     S.gram.as<double>(), S.Vbt2.as<float>(), s));
-      std::swap(S.Ub.p, S.Ub2.p);
-      std::swap(S.Vbt.p, S.Vbt2.p);
-      S.launches += 7;
+      // FP64 Newton refinement of the FP32 factors: three quadratically
+      // convergent steps separate the vectors of close singular values (the
+      // Jacobi leaves pairs 6e-5 apart mixed by ~2 %), so the convergence test
+      // reads FP64-accurate last entries of Ub, as with an FP64 SVD
+      BGPU_TRY(launch_svd_refine(S.B.as<double>(), m, S.Ub.as<float>(), S.Sb.as<float>(),
+                                 S.Vbt.as<float>(), S.ub_last.as<double>(),
+                                 S.sb64.as<double>(), S.oaw.as<double>(), kRefineSteps, s));
+      S.launches += 2 + 1 + 4 * kRefineSteps + 4;
     }
     BGPU_TRY(S.ev_end());
     BGPU_TRY(launch_restart_check(
-        S.Ub.as<float>(), S.Sb.as<float>(),
-        S.svd64 ? S.ub_last.as<double>() : nullptr,
-        S.svd64 ? S.sb64.as<double>() : nullptr, m, k, S.rem.as<float>(), g,
+        S.Ub.as<float>(), S.Sb.as<float>(), S.ub_last.as<double>(),
+        S.sb64.as<double>(), m, k, S.rem.as<float>(), g,
         o.tolerance, S.smax.as<float>(), kc, S.B.as<double>(),
         S.st.as<RestartStatus>(), S.trace ? S.ratios.as<float>() : nullptr, s));
     // restart status and the device error word in one stream round trip (no
@@ -678,10 +679,22 @@ extern "C" int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes) {
   return BGPU_OK;
 }
 
+extern "C" int bgpu_matrix_layout(const bgpu_matrix* mat, int* layout) {
+  BGPU_REQUIRE(mat && layout, BGPU_ERR_INVALID, "NULL argument");
+  *layout = mat->m.sell ? BGPU_LAYOUT_SELL
+                        : (mat->m.mode == kFloat ? BGPU_LAYOUT_FLOAT : BGPU_LAYOUT_PANELS);
+  return BGPU_OK;
+}
+
 extern "C" int bgpu_matrix_matvec(const bgpu_matrix* mat, const float* v,
                                   const float* sd, float* y, void* stream) {
   BGPU_REQUIRE(mat && v && y, BGPU_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  if (mat->m.sell) {
+    BGPU_TRY(launch_xv_sell(mat->m, v, sd, y, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));
+    return BGPU_OK;
+  }
   if (!(mat->m.stream_ok && mat->m.impl == 0))
     return launch_matvec(mat->m, v, sd, y, s);
   Buf err;
@@ -702,7 +715,9 @@ extern "C" int bgpu_matrix_rmatvec(const bgpu_matrix* mat, const float* u,
   BGPU_TRY(balloc(part, (size_t)mat->m.num_panels * mat->m.g * 4, false, s));
   Buf err;
   BGPU_TRY(balloc(err, 16, true, s));
-  if (mat->m.stream_ok && mat->m.impl == 0)
+  if (mat->m.sell)
+    BGPU_TRY(launch_xt_sell(mat->m, u, nullptr, nullptr, part.as<float>(), s));
+  else if (mat->m.stream_ok && mat->m.impl == 0)
     BGPU_TRY(launch_rmatvec_stream(mat->m, u, nullptr, nullptr, part.as<float>(),
                                    err.as<int>(), s));
   else

@@ -438,8 +438,6 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
       BGPU_CHECK_LAUNCH();
     }
   }
-  BGPU_TRY(dev_alloc(&m->colptr, (size_t)m->num_panels * (m->g + 1), &m->bytes, s));
-
   // indptr is validated (and the stream synchronised) before any kernel
   // reads entries through it.
   if (d->index_type == BGPU_INDEX_I64)
@@ -490,7 +488,22 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
     panel_rp.swap(rp);
   }
 
+  // Sliced-ELL layout for both products where it applies (counts, <= 4096
+  // genes); the packed CSR words were only its source then.
+  if (m->mode == kCounts) {
+    bool built = false;
+    BGPU_TRY(build_sell(m, s, &built));
+    if (built) {
+      BGPU_CUDA(cudaFreeAsync(m->csr_packed, s));
+      m->csr_packed = nullptr;
+      m->bytes -= std::max<size_t>(m->nnz_alloc * 4, 16);
+      BGPU_CUDA(cudaStreamSynchronize(s));  // temporaries are freed on return
+      return BGPU_OK;
+    }
+  }
+
   // Transposed copy.
+  BGPU_TRY(dev_alloc(&m->colptr, (size_t)m->num_panels * (m->g + 1), &m->bytes, s));
   const uint32_t num_sub = (uint32_t)ceil_div(m->n, kSubRows);
   const uint32_t subs_per_panel = m->P / kSubRows;
   DevBuf t_cnt;
@@ -680,10 +693,14 @@ int matrix_build_rows(Matrix* m, const bgpu_matrix_desc* d, const int64_t* rows,
 }
 
 void matrix_free(Matrix* m) {
-  void* ptrs[] = {m->rowptr, m->csr_packed, m->csr_val, m->csr_col,
-                  m->colptr, m->csc_packed, m->csc_val, m->csc_row,
-                  m->isf,    m->post,       m->sd,      m->rtab_r,
-                  m->rtab_c, m->csc16,      m->row_order};
+  void* ptrs[] = {m->rowptr,  m->csr_packed,  m->csr_val,   m->csr_col,
+                  m->colptr,  m->csc_packed,  m->csc_val,   m->csc_row,
+                  m->isf,     m->post,        m->sd,        m->rtab_r,
+                  m->rtab_c,  m->csc16,       m->row_order, m->xv_data,
+                  m->xv_grp,  m->xv_units,    m->xv_perm,   m->xv_isf,
+                  m->xv_post, m->xv_esc_n,    m->xv_esc_base, m->xv_esc,
+                  m->xt_data, m->xt_grp,      m->xt_units,  m->xt_gene,
+                  m->xt_pgrp, m->xt_esc_base, m->xt_esc};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   *m = Matrix();

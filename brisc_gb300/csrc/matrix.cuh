@@ -35,6 +35,44 @@ namespace bgpu {
 
 enum MatrixMode { kCounts = 0, kFloat = 1 };
 
+// Sliced-ELL views (sell.cu): scalar shape fields live in the Matrix, the
+// pointers are filled in per launch.
+struct XvView {  // X.v: 32-row groups, rows ordered by length
+  const uint2* data;         // units of four 16-bit entries, lane-interleaved
+  const uint32_t* grp;       // per group: first unit
+  const uint16_t* units;     // per group: units per lane
+  const int32_t* perm;       // position -> cell row (-1: padding)
+  const float* isf;          // per position
+  const float* post;         // per position (PFlog1pPF) or null
+  const uint16_t* esc_n;     // per position: counts >= 16 of the row
+  const uint32_t* esc_base;  // per position: first escape record
+  const uint32_t* esc;       // escape records gene << 16 | count
+  uint32_t groups;
+  uint32_t g;
+  uint64_t n;
+  uint64_t total_units;
+};
+struct XtView {  // X^T.u: (panel, gene) segments in 32-segment groups
+  const uint2* data;         // units of four 16-bit shared-memory offsets
+  const uint32_t* grp;       // per group: first unit
+  const uint16_t* units;     // per group: units per lane
+  const uint16_t* gene;      // per group and lane: gene (0xffff: none)
+  const uint32_t* pgrp;      // per panel: first group (panels + 1)
+  const uint32_t* esc_base;  // per panel: first escape record (panels + 1)
+  const uint32_t* esc;       // escape records local_row << 16 | count
+  const float* isf;
+  const float* post;
+  uint64_t n;
+  uint64_t total_units;
+  uint32_t g;
+  uint32_t P;                // rows per panel (<= 512)
+  uint32_t ppc;              // consecutive panels per CTA
+  uint32_t panels;
+  uint32_t ctas;             // CTAs of a launch = rows of the partials
+  uint32_t esc_max;          // most escapes in one panel
+  uint32_t groups;
+};
+
 // Per-cell table of normalised values for small counts:
 // tab[c] = log1pf(c * isf) for 1 <= c < 16 and tab[0] = 0.
 constexpr int kCountTab = 16;
@@ -84,6 +122,28 @@ struct Matrix {
   bool spmv_seg = false;   // X.v by the segmented stream (short rows) rather
                            // than 8 lanes per row
   int impl = 0;            // 0 = table-driven kernels, 1 = register-vector kernels
+
+  // Sliced-ELL layout (sell.cu), counts mode with g <= 4096: when `sell` is
+  // set both products run on it and the panel layout above is not built.
+  bool sell = false;
+  XvView xv{};
+  XtView xt{};
+  uint2* xv_data = nullptr;
+  uint32_t* xv_grp = nullptr;
+  uint16_t* xv_units = nullptr;
+  int32_t* xv_perm = nullptr;
+  float* xv_isf = nullptr;
+  float* xv_post = nullptr;
+  uint16_t* xv_esc_n = nullptr;
+  uint32_t* xv_esc_base = nullptr;
+  uint32_t* xv_esc = nullptr;
+  uint2* xt_data = nullptr;
+  uint32_t* xt_grp = nullptr;
+  uint16_t* xt_units = nullptr;
+  uint16_t* xt_gene = nullptr;
+  uint32_t* xt_pgrp = nullptr;
+  uint32_t* xt_esc_base = nullptr;
+  uint32_t* xt_esc = nullptr;
 };
 
 // Per-launch views passed by value to kernels.
@@ -161,6 +221,19 @@ bool compact16_supported(const Matrix& m);
 int build_compact16(Matrix* m, cudaStream_t s, uint64_t* bytes_acc);
 int launch_rmatvec16(const Matrix& m, const float* u, const float* u_scale,
                      float* u_out, float* partT, int* err, cudaStream_t s);
+
+// sell.cu: sliced-ELL layout and products. build_sell sets *built when the
+// layout applies (counts mode, g <= 4096, within its per-panel limits).
+bool sell_supported(const Matrix& m);
+int build_sell(Matrix* m, cudaStream_t s, bool* built);
+int launch_xv_sell(const Matrix& m, const float* v, const float* sd, float* y,
+                   cudaStream_t s);
+// X^T.u partials, gene-major: partT[gene * xt.ctas + cta] (reduced in CTA
+// order by launch_reduce_panels_t, with m.num_panels == xt.ctas).
+int launch_xt_sell(const Matrix& m, const float* u, const float* u_scale, float* u_out,
+                   float* partT, cudaStream_t s);
+// Per-gene FP64 moments: partials[cta * g + gene] = {sum, sum of squares}.
+int launch_xt_moments(const Matrix& m, double* partials, cudaStream_t s);
 
 // Bytes of the algorithmic traffic of one X.v / X^T.u launch (used for the
 // roofline figure). Counts what the chosen layout must stream.

@@ -232,6 +232,11 @@ __global__ void k_gene_sd(const double2* __restrict__ partials,
 }  // namespace
 
 double matvec_bytes(const Matrix& m) {
+  if (m.sell) {  // stream, per-position factors and descriptors, v, sd, y
+    const double npos = (double)m.xv.groups * 32.0;
+    return (double)m.xv.total_units * 8.0 + npos * (4.0 + 4.0 + 2.0) +
+           (m.post ? npos * 4.0 : 0.0) + m.xv.groups * 6.0 + m.g * 8.0 + m.n * 4.0;
+  }
   double per = m.mode == kCounts ? 4.0 : 6.0;
   double b = m.nnz * per + (m.n + 1) * 8.0 + m.n * 4.0 + m.g * 8.0;
   if (m.mode == kCounts) b += m.n * 4.0 * (m.post ? 2 : 1);
@@ -239,6 +244,11 @@ double matvec_bytes(const Matrix& m) {
 }
 
 double rmatvec_bytes(const Matrix& m) {
+  if (m.sell) {  // stream, descriptors, u (read and written scaled), isf, partials
+    const double groups = (double)m.xt.groups;
+    return (double)m.xt.total_units * 8.0 + m.n * 12.0 + (m.post ? m.n * 4.0 : 0.0) +
+           (double)m.xt.ctas * m.g * 4.0 + groups * 70.0 + m.xt.panels * 8.0;
+  }
   double per = m.mode == kCounts ? 4.0 : 6.0;
   double b = m.nnz * per + (double)m.num_panels * (m.g + 1) * 4.0 + m.n * 4.0 +
              (double)m.num_panels * m.g * 4.0;
@@ -302,6 +312,13 @@ int launch_rmatvec_partials(const Matrix& m, const float* u,
 
 int launch_gene_stddev(const Matrix& m, double* partials, float* sd,
                        cudaStream_t s) {
+  if (m.sell) {  // per-CTA moments over the sliced-ELL panels, CTA order
+    BGPU_TRY(launch_xt_moments(m, partials, s));
+    k_gene_sd<<<(unsigned)ceil_div(m.g, 256), 256, 0, s>>>(
+        (const double2*)partials, m.num_panels, m.g, m.n, sd);
+    BGPU_CHECK_LAUNCH();
+    return BGPU_OK;
+  }
   const CscView X = csc_view(m);
   const uint32_t cg = m.rmat_colgroup;
   dim3 grid(m.num_panels, (unsigned)ceil_div(m.g, cg));

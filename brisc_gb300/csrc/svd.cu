@@ -300,56 +300,143 @@ __global__ void k_f2d(const float* __restrict__ a, uint64_t n, double* __restric
   if (i < n) b[i] = (double)a[i];
 }
 
-// One Newton-Schulz (polar) step that restores the orthonormality of the
-// FP32 small-SVD factors: for m vectors x_i of length L (element r of x_i at
-// X[i * si + r * sr]), G = (x_i . x_j) - I accumulated in FP64, then
-// x_i <- x_i - 1/2 sum_j G[i][j] x_j (FP64, rounded once to FP32). The FP32
-// Jacobi leaves the factors orthonormal only to ~1e-6; the restart rotation
-// applies them to the Lanczos bases every restart, so without this the
-// bases drift by ~1e-6 per restart.
-__global__ void __launch_bounds__(256)
-k_gram64(const float* __restrict__ X, uint32_t m, uint32_t L, uint32_t si,
-         uint32_t sr, double* __restrict__ G) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t pairs = (uint64_t)m * m;
-  if (w >= pairs) return;
-  const uint32_t i = (uint32_t)(w / m), j = (uint32_t)(w % m);
-  if (j < i) return;  // symmetric: the (j, i) warp is not needed
+// ---------------------------------------------------------------------------
+// FP64 Newton refinement of the FP32 SVD (Ogita & Aishima, "Iterative
+// refinement for symmetric eigenvalue decomposition", 2018, Algorithm 1,
+// applied to B B^T = U diag(sigma^2) U^T). The FP32 Jacobi stops rotating a
+// pair once its columns are orthogonal to ~2.4e-6; for two singular values a
+// relative 6e-5 apart that leaves their vectors mixed by ~2 %, and the
+// convergence test reads exactly those vectors' last entries. Each step, in
+// FP64 with every product spread over many CTAs:
+//   W = B^T U, S = W^T W, R = I - U^T U, lam_i = S_ii / (1 - R_ii),
+//   E_ij = (S_ij + lam_j R_ij) / (lam_j - lam_i)   (i != j, when the pair is
+//          resolved: |numerator| < |lam_j - lam_i| / 4),
+//   E_ij = R_ij / 2 otherwise and on the diagonal,   U <- U + U E,
+// which converges quadratically; three steps take FP32-accurate factors to
+// FP64 accuracy. Then sigma_i = sqrt(lam_i) and Vbt's rows are (B^T U)_i /
+// sigma_i.
+__global__ void k_oa_w(const double* __restrict__ B, const double* __restrict__ U,
+                       uint32_t m, double* __restrict__ W) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)(m + 1) * m) return;
+  const uint32_t r = (uint32_t)(t % (m + 1)), i = (uint32_t)(t / (m + 1));
+  const double* b = B + (uint64_t)r * m;  // row r of B^T = column r of B
+  const double* u = U + (uint64_t)i * m;
   double acc = 0.0;
-  for (uint32_t r = lane; r < L; r += 32)
-    acc += (double)X[(uint64_t)i * si + (uint64_t)r * sr] *
-           (double)X[(uint64_t)j * si + (uint64_t)r * sr];
-  acc = warp_sum_t(acc);
-  if (lane == 0) {
-    const double v = acc - (i == j ? 1.0 : 0.0);
-    G[(uint64_t)i * m + j] = v;
-    G[(uint64_t)j * m + i] = v;
+  for (uint32_t c = 0; c < m; ++c) acc = fma(b[c], u[c], acc);
+  W[r + (uint64_t)i * (m + 1)] = acc;
+}
+
+__global__ void k_oa_sr(const double* __restrict__ W, const double* __restrict__ U,
+                        uint32_t m, double* __restrict__ S, double* __restrict__ R) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)m * m) return;
+  const uint32_t i = (uint32_t)(t % m), j = (uint32_t)(t / m);
+  const double* wi = W + (uint64_t)i * (m + 1);
+  const double* wj = W + (uint64_t)j * (m + 1);
+  double s = 0.0;
+  for (uint32_t r = 0; r <= m; ++r) s = fma(wi[r], wj[r], s);
+  const double* ui = U + (uint64_t)i * m;
+  const double* uj = U + (uint64_t)j * m;
+  double q = 0.0;
+  for (uint32_t c = 0; c < m; ++c) q = fma(ui[c], uj[c], q);
+  S[t] = s;
+  R[t] = (i == j ? 1.0 : 0.0) - q;
+}
+
+__global__ void __launch_bounds__(1024)
+k_oa_e(const double* __restrict__ S, const double* __restrict__ R, uint32_t m,
+       double* __restrict__ lam, double* __restrict__ E) {
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+    const uint64_t d = (uint64_t)i * m + i;
+    lam[i] = S[d] / (1.0 - R[d]);
+  }
+  __syncthreads();
+  for (uint64_t t = threadIdx.x; t < (uint64_t)m * m; t += blockDim.x) {
+    const uint32_t i = (uint32_t)(t % m), j = (uint32_t)(t / m);
+    double e = 0.5 * R[t];
+    if (i != j) {
+      const double num = S[t] + lam[j] * R[t];
+      const double den = lam[j] - lam[i];
+      if (fabs(num) < 0.25 * fabs(den)) e = num / den;
+    }
+    E[t] = e;
   }
 }
 
-__global__ void __launch_bounds__(256)
-k_ns_update(const float* __restrict__ X, uint32_t m, uint32_t L, uint32_t si,
-            uint32_t sr, const double* __restrict__ G, float* __restrict__ Y) {
+__global__ void k_oa_u(const double* __restrict__ U, const double* __restrict__ E,
+                       uint32_t m, double* __restrict__ Un) {
   const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (t >= (uint64_t)m * L) return;
-  const uint32_t i = (uint32_t)(t / L), r = (uint32_t)(t % L);
+  if (t >= (uint64_t)m * m) return;
+  const uint32_t r = (uint32_t)(t % m), i = (uint32_t)(t / m);
+  const double* e = E + (uint64_t)i * m;
+  double acc = U[t];
+  for (uint32_t c = 0; c < m; ++c) acc = fma(U[r + (uint64_t)c * m], e[c], acc);
+  Un[t] = acc;
+}
+
+__global__ void k_oa_out(const double* __restrict__ B, const double* __restrict__ U,
+                         const double* __restrict__ lam, uint32_t m,
+                         float* __restrict__ Ub, float* __restrict__ Sb,
+                         float* __restrict__ Vbt, double* __restrict__ ub_last,
+                         double* __restrict__ sb64) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)(m + 1) * m) return;
+  const uint32_t i = (uint32_t)(t % m), r = (uint32_t)(t / m);  // Vbt[i + r m]
+  const double sig = sqrt(fmax(lam[i], 0.0));
+  const double* b = B + (uint64_t)r * m;
+  const double* u = U + (uint64_t)i * m;
   double acc = 0.0;
-  const double* gi = G + (uint64_t)i * m;
-  for (uint32_t j = 0; j < m; ++j) acc += gi[j] * (double)X[(uint64_t)j * si + (uint64_t)r * sr];
-  const uint64_t o = (uint64_t)i * si + (uint64_t)r * sr;
-  Y[o] = (float)((double)X[o] - 0.5 * acc);
+  for (uint32_t c = 0; c < m; ++c) acc = fma(b[c], u[c], acc);
+  Vbt[t] = sig > 0.0 ? (float)(acc / sig) : 0.f;
+  if (r < m) Ub[(uint64_t)r + (uint64_t)i * m] = (float)U[(uint64_t)r + (uint64_t)i * m];
+  if (r == 0) {
+    Sb[i] = (float)sig;
+    sb64[i] = sig;
+    ub_last[i] = U[(uint64_t)(m - 1) + (uint64_t)i * m];
+  }
 }
 
 }  // namespace
 
-int launch_orthonormalize(const float* X, uint32_t m, uint32_t L, uint32_t si,
-                          uint32_t sr, double* G, float* Y, cudaStream_t s) {
-  const uint64_t warps = (uint64_t)m * m;
-  k_gram64<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, s>>>(X, m, L, si, sr, G);
+size_t svd_refine_doubles(uint32_t m) {
+  return 5ull * m * m + (uint64_t)(m + 1) * m + m;
+}
+
+int launch_svd_refine(const double* B, uint32_t m, float* Ub, float* Sb, float* Vbt,
+                      double* ub_last, double* sb64, double* work, int steps,
+                      cudaStream_t s) {
+  const uint64_t mm = (uint64_t)m * m;
+  double* U = work;
+  double* Un = U + mm;
+  double* Sm = Un + mm;
+  double* R = Sm + mm;
+  double* E = R + mm;
+  double* W = E + mm;
+  double* lam = W + (uint64_t)(m + 1) * m;
+  const unsigned gw = (unsigned)ceil_div((uint64_t)(m + 1) * m, 128);
+  const unsigned gm = (unsigned)ceil_div(mm, 128);
+  k_f2d<<<(unsigned)ceil_div(mm, 256), 256, 0, s>>>(Ub, mm, U);
   BGPU_CHECK_LAUNCH();
-  k_ns_update<<<(unsigned)ceil_div((uint64_t)m * L, 256), 256, 0, s>>>(X, m, L, si, sr,
-                                                                      G, Y);
+  for (int it = 0; it < steps; ++it) {
+    k_oa_w<<<gw, 128, 0, s>>>(B, U, m, W);
+    BGPU_CHECK_LAUNCH();
+    k_oa_sr<<<gm, 128, 0, s>>>(W, U, m, Sm, R);
+    BGPU_CHECK_LAUNCH();
+    k_oa_e<<<1, 1024, 0, s>>>(Sm, R, m, lam, E);
+    BGPU_CHECK_LAUNCH();
+    k_oa_u<<<gm, 128, 0, s>>>(U, E, m, Un);
+    BGPU_CHECK_LAUNCH();
+    std::swap(U, Un);
+  }
+  // the eigenvalues of the refined U: one more S diagonal
+  k_oa_w<<<gw, 128, 0, s>>>(B, U, m, W);
+  BGPU_CHECK_LAUNCH();
+  k_oa_sr<<<gm, 128, 0, s>>>(W, U, m, Sm, R);
+  BGPU_CHECK_LAUNCH();
+  k_oa_e<<<1, 1024, 0, s>>>(Sm, R, m, lam, E);
+  BGPU_CHECK_LAUNCH();
+  k_oa_out<<<gw, 128, 0, s>>>(B, U, lam, m, Ub, Sb, Vbt, ub_last, sb64);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -18,11 +18,14 @@ size_t jacobi_smem_bytes(uint32_t m, bool fp64);
 size_t jacobi_global_bytes(uint32_t m, bool fp64);
 float jacobi_threshold(uint32_t m);
 
-// One FP64-accumulated Newton-Schulz step on m vectors of length L (element r
-// of vector i at X[i * si + r * sr]): Y = X - X (X^T X - I) / 2, restoring
-// orthonormality to FP32 rounding. G: m * m doubles of scratch. Y != X.
-int launch_orthonormalize(const float* X, uint32_t m, uint32_t L, uint32_t si,
-                          uint32_t sr, double* G, float* Y, cudaStream_t s);
+// FP64 Newton (Ogita-Aishima) refinement of an FP32 SVD of B (FP64, m x
+// (m+1), column-major): `steps` steps on Ub, then Sb, Vbt and the FP64 last
+// row of Ub (ub_last) and singular values (sb64) from the refined factors.
+// Ub, Sb, Vbt are rewritten in place. work: svd_refine_doubles(m) doubles.
+size_t svd_refine_doubles(uint32_t m);
+int launch_svd_refine(const double* B, uint32_t m, float* Ub, float* Sb, float* Vbt,
+                      double* ub_last, double* sb64, double* work, int steps,
+                      cudaStream_t s);
 int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s);
 
 // One-sided Jacobi SVD of B (m x (m+1), column-major), in FP64 when Bd is

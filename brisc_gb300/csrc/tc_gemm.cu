@@ -34,6 +34,9 @@ namespace {
 
 constexpr int kTcThreads = 512;
 constexpr int kTcRows = 128;  // M of one MMA / rows per tile
+constexpr uint32_t kTcChunkK = 112;  // K per staging (A and B halves in smem)
+constexpr uint32_t kTcChunkN = 128;  // output columns per staging
+constexpr uint32_t kTcMaxK = 1024;
 
 struct TcLayout {
   uint32_t ahi, alo, bhi, blo, total;
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
           const float* __restrict__ Bm, uint64_t ldb, uint32_t ncols,
           float* __restrict__ C, uint64_t ldc, uint32_t Kp, uint32_t Np,
-          uint32_t tmem_cols, int* __restrict__ err) {
+          uint32_t tmem_cols, int accumulate, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
@@ -238,8 +241,12 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
       tmem_ld8(tmem + ((q * 32u) << 16) + c0, v);
       if (gr < rows) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (c0 + j < ncols) C[(uint64_t)(c0 + j) * ldc + gr] = v[j];
+        for (int j = 0; j < 8; ++j) {
+          if (c0 + j < ncols) {
+            float* cp = C + (uint64_t)(c0 + j) * ldc + gr;
+            *cp = accumulate ? *cp + v[j] : v[j];  // K chunks add in order
+          }
+        }
       }
     }
     tc_fence_before();
@@ -267,12 +274,9 @@ bool gemm_tc_supported(uint32_t K, uint32_t ncols) {
   return TcLayout(Kp, Np).total <= 227 * 1024;
 }
 
-int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
-                   const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
-                   uint64_t ldc, int* err, cudaStream_t s) {
-  if (rows == 0 || ncols == 0) return BGPU_OK;
-  BGPU_REQUIRE(gemm_tc_supported(K, ncols), BGPU_ERR_UNSUPPORTED,
-               "tensor-core rotation needs K, ncols <= 256 within shared memory");
+static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                           const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
+                           uint64_t ldc, int accumulate, int* err, cudaStream_t s) {
   const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 31) & ~31u;
   uint32_t tcols = 32;
   while (tcols < Np) tcols <<= 1;
@@ -282,8 +286,33 @@ int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
   const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
   const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)num_sms());
   k_gemm_tc<<<grid, kTcThreads, smem, s>>>(A, lda, rows, K, Bm, ldb, ncols, C, ldc,
-                                           Kp, Np, tcols, err);
+                                           Kp, Np, tcols, accumulate, err);
   BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+// Subspaces larger than one staging (K > 112 or more than 128 output columns,
+// the 10M-cell solve's m = 200) run as K chunks of <= 112 and column chunks
+// of <= 128: each chunk's operands fit the 227 KB of shared memory, and the
+// K chunks of a column chunk add into C in chunk order (fixed, so the result
+// is the same on every run).
+int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                   const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
+                   uint64_t ldc, int* err, cudaStream_t s) {
+  if (rows == 0 || ncols == 0) return BGPU_OK;
+  BGPU_REQUIRE(K >= 1 && ncols <= K && K <= kTcMaxK, BGPU_ERR_UNSUPPORTED,
+               "tensor-core rotation needs 1 <= ncols <= K <= 1024");
+  if (gemm_tc_supported(K, ncols))
+    return launch_tc_chunk(A, lda, rows, K, Bm, ldb, ncols, C, ldc, 0, err, s);
+  for (uint32_t n0 = 0; n0 < ncols; n0 += kTcChunkN) {
+    const uint32_t nc = std::min(kTcChunkN, ncols - n0);
+    for (uint32_t k0 = 0; k0 < K; k0 += kTcChunkK) {
+      const uint32_t kk = std::min(kTcChunkK, K - k0);
+      BGPU_TRY(launch_tc_chunk(A + (uint64_t)k0 * lda, lda, rows, kk,
+                               Bm + (uint64_t)n0 * ldb + k0, ldb, nc,
+                               C + (uint64_t)n0 * ldc, ldc, k0 > 0 ? 1 : 0, err, s));
+    }
+  }
   return BGPU_OK;
 }
 

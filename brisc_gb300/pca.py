@@ -197,6 +197,13 @@ class DeviceMatrix:
 
     __del__ = close
 
+    @property
+    def layout(self) -> str:
+        """'sell' (sliced-ELL products), 'panels' or 'float'."""
+        v = C.c_int()
+        L.call("bgpu_matrix_layout", self.handle, C.byref(v))
+        return {0: "panels", 1: "sell", 2: "float"}[v.value]
+
     def device_bytes(self) -> int:
         b = C.c_uint64()
         L.call("bgpu_matrix_bytes", self.handle, C.byref(b))

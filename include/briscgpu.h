@@ -122,6 +122,16 @@ BGPU_API int bgpu_matrix_destroy(bgpu_matrix* mat);
 /* Device bytes held by the matrix layout. */
 BGPU_API int bgpu_matrix_bytes(const bgpu_matrix* mat, uint64_t* bytes);
 
+/* Which layout (and so which product kernels) the matrix was built with. No
+ * counterpart in the reference (its products read the caller's CSR/CSC). */
+enum {
+  BGPU_LAYOUT_PANELS = 0,  /* counts: packed CSR words + row-panel transpose   */
+  BGPU_LAYOUT_SELL = 1,    /* counts, <= 4096 genes: sliced-ELL rows for X.v
+                              and sliced-ELL (panel, gene) segments for X^T.u  */
+  BGPU_LAYOUT_FLOAT = 2    /* pre-normalised float32 values                    */
+};
+BGPU_API int bgpu_matrix_layout(const bgpu_matrix* mat, int* layout);
+
 /* y = X . (v / sd)   (brisc/pca.pyx:440-475; no centring). Device pointers.
  * sd may be NULL (treated as all ones). y has num_cells entries. */
 BGPU_API int bgpu_matrix_matvec(const bgpu_matrix* mat, const float* v, const float* sd,
@@ -151,10 +161,10 @@ typedef struct bgpu_solve_opts {
                                 Kahan-Parlett); 1 = one pass always;
                                 2 = two passes always (CGS2). The V side
                                 follows the same rule.                          */
-  uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor cores
-                                when subspace_size <= 104, else SIMT),
-                                1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass TF32
-                                split GEMM with FP32 accumulation                */
+  uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor
+                                cores), 1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass
+                                TF32 split GEMM with FP32 accumulation (K /
+                                column chunks beyond 112 / 128)                  */
   volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
                                 NULL (replaces PyErr_CheckSignals, pca.pyx:1173) */
   int use_graphs;            /* reserved for CUDA-graph replay of the Lanczos
@@ -227,7 +237,8 @@ BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_hos
  * reference's matmul_nn_f_out at pca.pyx:578-616, U <- U . Ub[:, :kc]).
  * Device pointers, all column-major: A rows x K (lda), Bm K x >= ncols (ldb),
  * C rows x ncols (ldc). mode 1: FP32 SIMT; mode 2: tensor cores (tcgen05,
- * 3-pass TF32 split, FP32 accumulation; K, ncols <= 104). Synchronous. */
+ * 3-pass TF32 split, FP32 accumulation; K > 112 or ncols > 128 run as
+ * chunks whose K parts add in a fixed order). Synchronous. */
 BGPU_API int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
                                uint32_t K, const float* Bm, uint64_t ldb,
                                uint32_t ncols, float* C, uint64_t ldc, int mode,

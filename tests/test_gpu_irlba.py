@@ -13,7 +13,7 @@ import scipy.sparse as sp
 
 import brisc_gb300 as bg
 from brisc_gb300 import DeviceMatrix, _lib
-from brisc_gb300.synth import nb_counts
+from synth import nb_counts
 from oracle import dense
 from oracle import irlba as oirlba
 
@@ -228,7 +228,7 @@ def test_large_solve_meets_fp64_gate(cuda):
     Gram-Schmidt, tensor-core rotation): relative singular-value error <= 1e-4
     against the FP64
     Gram-matrix oracle, and the solve converges."""
-    from brisc_gb300.synth import nb_counts
+    from synth import nb_counts
     c = nb_counts(200_000, 2000, seed=0, density=0.05)
     M = DeviceMatrix(c.indptr.astype(np.int32), c.indices, c.data, c.num_cells, 2000,
                      norm="logCP10k", inv_size_factors=c.isf)

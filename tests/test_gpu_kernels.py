@@ -11,7 +11,7 @@ import pytest
 import scipy.sparse as sp
 
 from brisc_gb300 import DeviceMatrix, _lib
-from brisc_gb300.synth import nb_counts
+from synth import nb_counts
 from oracle import clib, dense
 
 pytestmark = pytest.mark.gpu
@@ -212,10 +212,14 @@ def test_small_svd(cuda, m):
 
 
 @pytest.mark.parametrize("rows,K,ncols", [(5000, 100, 99), (5000, 100, 100),
-                                          (1000, 100, 37), (300, 7, 3), (128, 64, 1)])
+                                          (1000, 100, 37), (300, 7, 3), (128, 64, 1),
+                                          # K / column chunks (the m = 200 solve)
+                                          (5000, 200, 199), (3000, 150, 129),
+                                          (777, 256, 256), (1000, 113, 5)])
 def test_rotate_basis_tensor_cores(cuda, rows, K, ncols):
     """U . Ub[:, :kc] on the tensor cores (3-pass TF32 split) against the SIMT
-    FP32 GEMM and an FP64 product: both within 2e-6 of the FP64 scale."""
+    FP32 GEMM and an FP64 product: both within 2e-6 of the FP64 scale (the
+    chunked shapes add their K parts in FP32, in chunk order)."""
     import torch
     rng = np.random.default_rng(rows + K + ncols)
     lda = rows + 64 - rows % 64
