@@ -4,10 +4,15 @@ Requests (a count matrix on the host plus solve parameters) arrive at any
 time. A dispatcher admits them in arrival order, first fit: the first waiting
 request whose estimated device footprint fits in the HBM budget left by the
 running ones starts as soon as a slot is free, so small requests flow past a
-large one that is waiting for memory. Each slot is a host thread with its own
-CUDA stream; it uploads the request, builds its device layout, solves and
-returns the PCs. Requests that arrive while others run overlap with them on
-the device.
+large one that is waiting for memory. Past `max_wait` seconds of waiting the
+oldest request stops being overtaken: nothing else starts until it fits, so a
+steady stream of small requests cannot starve a large one. Each slot is a
+host thread with its own CUDA stream; it uploads the request, builds its
+device layout, solves and returns the PCs. Requests that arrive while others
+run overlap with them on the device. A solve that fails to allocate device
+memory (the footprint model under-estimated it, or memory outside the server
+is in use) goes back to the head of the queue with a larger footprint, up to
+`max_retries` times.
 
 Every solve is deterministic and independent of what else runs, so a
 request's result is bit-identical alone and in the mix (the tests check this).
@@ -56,17 +61,19 @@ class PCARequest:
 
 
 def footprint_bytes(num_cells: int, num_genes: int, nnz: int, m: int) -> int:
-    """Device bytes one request holds at its peak: the staged inputs and the
-    layout build, the resident layout and the solver state (with 10 %
-    margin)."""
+    """Device bytes one request holds at its peak (with 10 % margin): the
+    staged inputs and build temporaries of the sliced-ELL layout (packed CSR
+    words, per-panel segment tables), the resident layout (2-byte entries of
+    both copies with their padding, per-row and per-segment descriptors) and
+    the solver state (two n x m and two g x m bases, partials)."""
     n, g = int(num_cells), int(num_genes)
-    panels = (n + 1023) // 1024
+    panels = (n + 511) // 512 + 1
     ld_n = (n + 63) // 64 * 64
-    build = nnz * (2 + 4) + (n + 1) * 8 + ((n + 255) // 256) * g * 4
-    layout = (nnz + 8) * 4 * 2 + (n + 5) * 8 + n * 4 * 2 + n * 16 * 4 * 2 \
-        + panels * (g + 1) * 4
+    build = nnz * (6 + 4) + (n + 1) * 8 + n * 8 + panels * g * 12
+    layout = int(nnz * 2 * 2.4) + n * 30 + panels * g * 4 + (n + 5) * 8
     solver = 2 * ld_n * m * 4 + 2 * g * m * 4 + 2 * ld_n * 4 \
-        + ((n + 255) // 256) * (m + 2) * 4 + panels * g * 4 * 5 + n * m * 4
+        + ((n + 255) // 256) * (m + 2) * 4 + panels * g * 4 * 5 + n * m * 4 \
+        + m * m * 64
     return int((build + layout + solver) * 1.1) + (16 << 20)
 
 
@@ -90,6 +97,19 @@ class _Pending:
     fut: Future
     arrival: float
     footprint: int
+    retries: int = 0
+
+
+def _out_of_memory(e: BaseException) -> bool:
+    """A device allocation failure of the library (BGPU_ERR_ALLOC) or of torch."""
+    from ._lib import ERR_ALLOC, BriscGPUError
+    if isinstance(e, BriscGPUError) and e.code == ERR_ALLOC:
+        return True
+    try:
+        import torch
+        return isinstance(e, torch.cuda.OutOfMemoryError)
+    except (ImportError, AttributeError):  # pragma: no cover
+        return False
 
 
 def gpu_solve(req: PCARequest, stream) -> SolveResult:
@@ -113,15 +133,22 @@ class PCAServer:
 
     slots: solves that may run at once. hbm_budget: device bytes the running
     solves may hold together (default: 80 % of the free memory at start).
-    solve_fn(request, stream) -> SolveResult does the work (default: the GPU
-    solve); make_stream() gives each slot its stream.
+    max_wait: seconds after which the oldest waiting request is no longer
+    overtaken (None: pure first fit). max_retries: how often a request whose
+    solve ran out of device memory is queued again. solve_fn(request,
+    stream) -> SolveResult does the work (default: the GPU solve);
+    make_stream() gives each slot its stream.
     """
 
     def __init__(self, slots: int = 8, hbm_budget: int | None = None,
                  solve_fn: Callable | None = None,
-                 make_stream: Callable | None = None):
+                 make_stream: Callable | None = None,
+                 max_wait: float | None = 10.0, max_retries: int = 3):
         if slots < 1:
             raise ValueError("slots must be >= 1")
+        self.max_wait = max_wait
+        self.max_retries = int(max_retries)
+        self.requeued = 0
         if hbm_budget is None:
             import torch
             hbm_budget = int(torch.cuda.mem_get_info()[0] * 0.8)
@@ -180,9 +207,17 @@ class PCAServer:
 
     # -- internals ---------------------------------------------------------
     def _pick(self) -> _Pending | None:
-        if self._running >= self.slots:
+        if self._running >= self.slots or not self._pending:
             return None
         room = self.budget - self._committed
+        head = min(self._pending, key=lambda p: p.arrival)
+        if self.max_wait is not None and \
+                time.perf_counter() - head.arrival > self.max_wait:
+            # the oldest request has waited long enough: it goes next
+            if head.footprint <= room:
+                self._pending.remove(head)
+                return head
+            return None
         for i, p in enumerate(self._pending):
             if p.footprint <= room:
                 return self._pending.pop(i)
@@ -197,7 +232,8 @@ class PCAServer:
                         break
                     if self._closing and not self._pending and self._running == 0:
                         return
-                    self._cv.wait()
+                    # wake up to re-check the waiting time of the oldest request
+                    self._cv.wait(timeout=0.05 if self._pending else None)
                 self._committed += p.footprint
                 self._running += 1
                 self.max_committed = max(self.max_committed, self._committed)
@@ -215,11 +251,20 @@ class PCAServer:
         except BaseException as e:  # noqa: BLE001 - returned to the caller
             err = e
         finish = time.perf_counter()
+        retry = (err is not None and _out_of_memory(err)
+                 and p.retries < self.max_retries)
         with self._cv:
             self._committed -= p.footprint
             self._running -= 1
+            if retry:  # back to the queue, oldest first, with a larger estimate
+                p.retries += 1
+                p.footprint = min(int(p.footprint * 1.5), self.budget)
+                self._pending.insert(0, p)
+                self.requeued += 1
             self._cv.notify_all()
-        p.fut.set_result(PCAResponse(res, err, p.arrival, start, finish, p.footprint))
+        if not retry:
+            p.fut.set_result(PCAResponse(res, err, p.arrival, start, finish,
+                                         p.footprint))
 
 
 def percentile(xs, q: float) -> float:

@@ -12,6 +12,12 @@ reference's outputs, so the tests never regenerate data:
 * tocsc.npz      csr_tocsc (brisc/cysparse.pyx:1179) of the same matrix.
 * irlba.npz      irlba PCs (brisc/pca.pyx:661) on clustered NB matrices whose
                  top singular values are separated, plus one flat-spectrum case.
+* parity50k.npz  irlba at the 50,000 x 2,000 configuration (50 PCs, subspace
+                 100, seed 0) on the flat and the 13-cluster NB matrix: the
+                 singular values, the right vectors A^T PCs / s^2 (genes x 50,
+                 FP64 from the reference's PCs), the convergence flag, the
+                 reference's own accuracy against the FP64 oracle, and a
+                 fingerprint of the seeded input.
 * hvg.npz        gene_mean_and_variance_csr/_csc and clipped_sum_csr/_csc
                  (brisc/hvg.pyx) on an NB count matrix with a few large
                  counts, over all cells and over a cell subset, uint32 and
@@ -19,6 +25,7 @@ reference's outputs, so the tests never regenerate data:
 
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py hvg      # hvg.npz only
+    python tests/golden/make_golden.py parity   # parity50k.npz only
 """
 from __future__ import annotations
 
@@ -30,7 +37,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from brisc_gb300.synth import nb_counts  # noqa: E402
+from synth import nb_counts  # noqa: E402
 from oracle import ref  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
@@ -82,11 +89,40 @@ def make_hvg(M) -> None:
     np.savez_compressed(OUT / "hvg.npz", **out)
 
 
+def make_parity() -> None:
+    import json
+    from oracle import accuracy as A
+    out = {}
+    for name in A.PARITY_CASES:
+        c, xn = A.parity_input(name)
+        n, g, k, m = c.num_cells, c.num_genes, 50, 100
+        ip32, ix32 = c.indptr.astype(np.int32), c.indices.astype(np.int32)
+        pcs, conv = ref.run_irlba(ip32, ix32, xn, n, g, k, m, 1e-6, 100, seed=0,
+                                  num_threads=8, match_parallel=False)
+        ip, ix = c.indptr.astype(np.int64), c.indices.astype(np.int64)
+        mean, sd = A.gene_moments64(ip, ix, xn, n, g)
+        G = A.gram64(ip, ix, xn, n, g, mean, sd)
+        S, V = A.truth(G, k + 1)
+        Vr = A.right_vectors(ip, ix, xn, n, g, mean, sd, pcs)
+        rep = A.solution_report(pcs, Vr, S, V, G, k)
+        out[f"{name}_fingerprint"] = A.fingerprint(c.indptr, c.indices, c.data)
+        out[f"{name}_S"] = np.linalg.norm(pcs.astype(np.float64), axis=0)
+        out[f"{name}_V"] = Vr.astype(np.float32)
+        out[f"{name}_converged"] = np.array(conv)
+        out[f"{name}_report"] = np.array(json.dumps(rep))
+        print(name, "converged", conv, "max rel sv", rep["max_rel_sv_error"],
+              "gapped", rep["gapped_j"], "max top-j angle", rep["max_top_j_angle"])
+    np.savez_compressed(OUT / "parity50k.npz", **out)
+
+
 def main() -> int:
     M = ref.load()
     if M is None:
         print("reference modules unavailable", file=sys.stderr)
         return 1
+    if sys.argv[1:] == ["parity"]:
+        make_parity()
+        return 0
     if "hvg" in M:
         make_hvg(M)
     if sys.argv[1:] == ["hvg"]:
