@@ -78,6 +78,8 @@ def parse():
                     help="skip the FP64 accuracy report of the CPU-baseline leg")
     ap.add_argument("--accuracy", action="store_true",
                     help="FP64 accuracy report even with --no-cpu-baseline")
+    ap.add_argument("--rotation-mode", type=int, default=0,
+                    help="restart rotation of U: 0 default, 1 FP32 SIMT, 2 tensor cores")
     ap.add_argument("--reorth-passes", default="auto",
                     type=lambda x: x if x == "auto" else int(x),
                     help="U-side Gram-Schmidt passes: auto (adaptive), 1 or 2")
@@ -379,7 +381,8 @@ def run_ours(args):
                      inv_size_factors=C.isf, stream=stream)
     pcs_dev = torch.empty((n, k), dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
-        r = M.solve(k, m, reorth_passes=args.reorth_passes, PCs=pcs_dev,
+        r = M.solve(k, m, reorth_passes=args.reorth_passes,
+                    rotation_mode=args.rotation_mode, PCs=pcs_dev,
                     stream=stream)
     barrier()
     torch.cuda.synchronize()
@@ -389,7 +392,8 @@ def run_ours(args):
         stop = torch.cuda.Event(enable_timing=True)
         start.record(stream)
         for _ in range(args.steps):
-            r = M.solve(k, m, reorth_passes=args.reorth_passes, PCs=pcs_dev,
+            r = M.solve(k, m, reorth_passes=args.reorth_passes,
+                        rotation_mode=args.rotation_mode, PCs=pcs_dev,
                         profile=True, stream=stream)
             infos.append(r.info)
         stop.record(stream)
@@ -422,7 +426,8 @@ def run_ours(args):
         Me = DeviceMatrix(np_views[0], np_views[1], np_views[2], n, g,
                           norm="logCP10k", inv_size_factors=np_views[3],
                           stream=stream)
-        Me.solve(k, m, reorth_passes=args.reorth_passes, PCs=np_views[4],
+        Me.solve(k, m, reorth_passes=args.reorth_passes,
+                 rotation_mode=args.rotation_mode, PCs=np_views[4],
                  stream=stream)
         Me.close()
     torch.cuda.synchronize()

@@ -80,12 +80,14 @@ int launch_gemm_ts(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                    bool c_rowmajor, cudaStream_t s);
 
 // C = A . Bm[:, :ncols] on the tensor cores (tc_gemm.cu): A rows x K and Bm
-// (K x ncols, ldb) column-major, C column-major (ldc); 3-pass TF32 split with
-// FP32 accumulation. err receives a device error word on a timed-out wait.
+// (K x ncols, ldb) column-major, C column-major (ldc); 3 x BF16 split with
+// FP32 accumulation, dominated columns of Bm in the pivoted delta form.
+// Scratch: dwork K x ncols floats, piv ncols ints. err receives a device
+// error word on a timed-out wait.
 bool gemm_tc_supported(uint32_t K, uint32_t ncols);
 int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                    const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
-                   uint64_t ldc, int* err, cudaStream_t s);
+                   uint64_t ldc, float* dwork, int* piv, int* err, cudaStream_t s);
 
 // B (m x (m+1), column-major FP64) -> float copy for the small SVD.
 int launch_b_to_float(const double* B, uint32_t m, float* Bf, cudaStream_t s);

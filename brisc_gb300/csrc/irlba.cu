@@ -163,10 +163,10 @@ struct Solver {
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
       Vbt, oaw, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
-      sb64, ratios,
+      sb64, ratios, rotd, rotpiv,
       derr, taken, ticket;
   bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
-  int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3xTF32
+  int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3 x BF16
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
   HostStatus hst;
 
@@ -253,6 +253,8 @@ struct Solver {
     BGPU_TRY(balloc(Ub, (size_t)m * m * 4, true, s));
     BGPU_TRY(balloc(Sb, (size_t)m * 4, true, s));
     BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
+    BGPU_TRY(balloc(rotd, (size_t)m * m * 4, false, s));  // tensor-core rotation scratch
+    BGPU_TRY(balloc(rotpiv, (size_t)m * 4, false, s));
     BGPU_TRY(balloc(oaw, svd_refine_doubles(m) * 8, true, s));
     if (jacobi_smem_bytes(m, svd64) > 220 * 1024)
       BGPU_TRY(balloc(svdwork, jacobi_global_bytes(m, svd64), true, s));
@@ -514,7 +516,8 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     BGPU_TRY(S.ev_begin(5));
     if (S.rot_mode == 2)
       BGPU_TRY(launch_gemm_tc(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), m, kc,
-                              S.Unew.as<float>(), S.ldu, S.derr.as<int>(), s));
+                              S.Unew.as<float>(), S.ldu, S.rotd.as<float>(),
+                              S.rotpiv.as<int>(), S.derr.as<int>(), s));
     else
       BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1,
                               m, nullptr, kc, S.Unew.as<float>(), S.ldu, false, s));
@@ -763,9 +766,12 @@ extern "C" int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
     BGPU_TRY(launch_gemm_ts(A, lda, rows, K, Bm, 1, ldb, nullptr, ncols, C, ldc,
                             false, s));
   else {
-    Buf err;
+    Buf err, dwork, piv;
     BGPU_TRY(balloc(err, 16, true, s));
-    BGPU_TRY(launch_gemm_tc(A, lda, rows, K, Bm, ldb, ncols, C, ldc, err.as<int>(), s));
+    BGPU_TRY(balloc(dwork, (size_t)K * ncols * 4, false, s));
+    BGPU_TRY(balloc(piv, (size_t)ncols * 4, false, s));
+    BGPU_TRY(launch_gemm_tc(A, lda, rows, K, Bm, ldb, ncols, C, ldc, dwork.as<float>(),
+                            piv.as<int>(), err.as<int>(), s));
     int h = 0;
     BGPU_CUDA(cudaMemcpyAsync(&h, err.p, 4, cudaMemcpyDeviceToHost, s));
     BGPU_CUDA(cudaStreamSynchronize(s));

@@ -3,28 +3,50 @@
 // cores: tcgen05.mma with operands in shared memory and the accumulator in
 // tensor memory (TMEM).
 //
-// Precision: FP32 operands are split as x = hi + lo with hi = x truncated to
-// TF32 (low 13 mantissa bits cleared) and lo = x - hi (exact in FP32); the
-// product is hi.hi + hi.lo + lo.hi (three kind::tf32 MMAs accumulated in FP32
-// in TMEM). The dropped lo.lo term and the TF32 reading of lo are below 2^-20
-// relative per product, so the rotation keeps FP32-level accuracy while the
-// tensor pipe carries the arithmetic (the rotation's ~25 flop/byte would need
-// ~170 TFLOP/s of FP32 to keep up with HBM).
+// Precision: 3 x BF16 split products accumulated in FP32. Each FP32 operand
+// is split x = x1 + x2 + x3 with x1 = bf16(x), x2 = bf16(x - x1), x3 =
+// bf16(x - x1 - x2) (round to nearest; both differences are exact in FP32),
+// which carries 24 significant bits. Six kind::f16 MMAs per K step form
+// x1y1 + x1y2 + x2y1 + x1y3 + x2y2 + x3y1; the dropped terms are below 2^-24
+// relative per product and unbiased. The tensor pipe carries the arithmetic:
+// the rotation's ~25 flop/byte would need ~170 TFLOP/s of FP32 to keep up
+// with HBM.
+//
+// The tensor core's FP32 accumulation does not round to nearest: measured on
+// GB300, a 100-term rotation of unit columns comes out 5e-7 to 8e-7 short in
+// relative norm (4-6 ulp, always toward zero), where an FP32 FMA loop is
+// unbiased. The restart applies the rotation to the same converged Ritz
+// vectors every restart, so that shrinkage compounds (5e-5 relative
+// singular-value error after the 69 restarts of the 1M-cell solve, 2.8e-7
+// with an FP32 FMA rotation). Two measures keep the bias off the result:
+//  - pivoted delta: an output column i whose rotation column is dominated by
+//    one entry (|Ub[p, i]| >= 1/2; a converged Ritz vector's column is e_p up
+//    to small mixing) is computed as U . (Ub[:, i] - sign e_p) on the tensor
+//    cores plus sign U[:, p], added in the epilogue in FP32 (one
+//    round-to-nearest add). The biased part then scales with the mixing,
+//    not with the vector; a column that is exactly e_p is copied exactly;
+//  - the five small cross products of every K step are accumulated first and
+//    the x1y1 products last, so the small terms are not truncated against
+//    large partial sums.
+// The MMAs and the epilogue adds run in a fixed order: the result is the
+// same on every run.
 //
 // Shape: persistent CTAs (one per SM, 512 threads) walk 128-row tiles of U.
-// Ub's split halves are staged once per CTA; each tile of U is loaded with
+// Ub's three parts are staged once per CTA; each tile of U is loaded with
 // coalesced 32-byte row runs into registers, split and written in the
-// canonical no-swizzle K-major layout (8-row x 16-byte core matrices,
-// K-direction core stride LBO = 128 B, 8-row stride SBO = Kp/4 * 128 B); one
-// elected thread issues 3 * Kp/8 MMAs of M=128, N=Np, K=8 and commits them to
-// an mbarrier. The next tile's loads are issued right after the MMAs, so they
-// are in flight while the MMAs run and while all 16 warps read the
-// accumulator back (tcgen05.ld, 32 lanes x 8 columns per load) and store C
-// column-major (128-byte runs per column).
+// canonical no-swizzle K-major layout (8-row x 16-byte core matrices of 8
+// BF16, K-direction core stride LBO = 128 B, 8-row stride SBO = Kp/8 * 128
+// B); one elected thread issues 6 * Kp/16 MMAs of M=128, N=Np, K=16 and
+// commits them to an mbarrier. The next tile's loads are issued right after
+// the MMAs, so they are in flight while the MMAs run and while all 16 warps
+// read the accumulator back (tcgen05.ld, 32 lanes x 8 columns per load) and
+// store C column-major (128-byte runs per column).
 //
 // Every mbarrier wait is bounded (about 1 s of SM clock): on timeout the
 // kernel records kDevErrTimeout, stops, frees its TMEM and returns.
 #include <algorithm>
+
+#include <cuda_bf16.h>
 
 #include "dense.cuh"
 #include "tma.cuh"
@@ -38,14 +60,14 @@ constexpr uint32_t kTcChunkK = 112;  // K per staging (A and B halves in smem)
 constexpr uint32_t kTcChunkN = 128;  // output columns per staging
 constexpr uint32_t kTcMaxK = 1024;
 
-struct TcLayout {
-  uint32_t ahi, alo, bhi, blo, total;
+struct TcLayout {  // three BF16 parts of the A tile and of B
+  uint32_t a[3], b[3], total;
   __host__ __device__ TcLayout(uint32_t Kp, uint32_t Np) {
-    ahi = 1024;  // mbarrier + TMEM address slot live below
-    alo = ahi + kTcRows * Kp * 4;
-    bhi = alo + kTcRows * Kp * 4;
-    blo = bhi + Np * Kp * 4;
-    total = blo + Np * Kp * 4;
+    a[0] = 1024;  // mbarrier + TMEM address slot live below
+    for (int i = 1; i < 3; ++i) a[i] = a[i - 1] + kTcRows * Kp * 2;
+    b[0] = a[2] + kTcRows * Kp * 2;
+    for (int i = 1; i < 3; ++i) b[i] = b[i - 1] + Np * Kp * 2;
+    total = b[2] + Np * Kp * 2;
   }
 };
 
@@ -60,17 +82,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo,
   return d;
 }
 
-// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_tf32(uint32_t M, uint32_t N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b,
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b,
                                          uint32_t idesc, uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
       ::"r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accum)
       : "memory");
 }
@@ -102,40 +124,82 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Split 4 floats into TF32 high parts and FP32 remainders.
-__device__ __forceinline__ void split4(const float (&x)[4], uint4& hi, uint4& lo) {
-  uint32_t h[4], l[4];
+// Split 8 floats into three BF16 parts (round to nearest at each stage; the
+// differences are exact in FP32), packed 8 per 16 bytes in k order.
+__device__ __forceinline__ void split8(const float (&x)[8], uint4 (&p)[3]) {
+  uint32_t w[3][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    h[i] = __float_as_uint(x[i]) & 0xFFFFE000u;
-    l[i] = __float_as_uint(x[i] - __uint_as_float(h[i]));
+    float2 r = make_float2(x[2 * i], x[2 * i + 1]);
+#pragma unroll
+    for (int part = 0; part < 3; ++part) {
+      const __nv_bfloat162 h = __float22bfloat162_rn(r);
+      const float2 f = __bfloat1622float2(h);
+      r = make_float2(r.x - f.x, r.y - f.y);
+      w[part][i] = *reinterpret_cast<const uint32_t*>(&h);
+    }
   }
-  hi = make_uint4(h[0], h[1], h[2], h[3]);
-  lo = make_uint4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+  for (int part = 0; part < 3; ++part)
+    p[part] = make_uint4(w[part][0], w[part][1], w[part][2], w[part][3]);
 }
 
-// Byte offset of element (row, 4*kg) in the core-matrix layout (16 bytes
-// hold k = 4kg..4kg+3 of one row).
+// Byte offset of element (row, 8*kg) in the core-matrix layout (16 bytes
+// hold k = 8kg..8kg+7 of one row).
 __device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t kg, uint32_t kq) {
   return ((row >> 3) * kq + kg) * 128u + (row & 7u) * 16u;
 }
 
 // Tasks per thread when a tile's A values are staged in registers: one task
-// is 4 consecutive k of one row (128 rows x Kp/4 tasks, Kp <= 112).
-constexpr int kTcTasks = (kTcRows * 28 + kTcThreads - 1) / kTcThreads;
+// is 8 consecutive k of one row (128 rows x Kp/8 tasks, Kp <= 112).
+constexpr int kTcTasks = (kTcRows * 14 + kTcThreads - 1) / kTcThreads;
 
+// Pivots of the delta form: for column i of Bm (K x ncols, ldb), p = the
+// row of its largest |entry| (lowest row on ties); when |Bm[p, i]| >= 1/2,
+// piv[i] = +-(p + 1) (the entry's sign) and D[:, i] = Bm[:, i] - sign e_p
+// (exact in FP32), else piv[i] = 0 and D[:, i] = Bm[:, i]. D has ld = K.
+// One warp per column.
+__global__ void __launch_bounds__(256)
+k_rot_pivots(const float* __restrict__ Bm, uint64_t ldb, uint32_t K, uint32_t ncols,
+             float* __restrict__ D, int* __restrict__ piv) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (col >= ncols) return;
+  const float* b = Bm + (uint64_t)col * ldb;
+  float best = -1.f;
+  uint32_t arg = 0;
+  for (uint32_t r = lane; r < K; r += 32) {
+    const float a = fabsf(b[r]);
+    if (a > best) { best = a; arg = r; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const uint32_t oa = __shfl_xor_sync(0xffffffffu, arg, o);
+    if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+  }
+  const bool use = best >= 0.5f;
+  const float sgn = b[arg] < 0.f ? -1.f : 1.f;
+  for (uint32_t r = lane; r < K; r += 32)
+    D[(uint64_t)col * K + r] = (use && r == arg) ? b[r] - sgn : b[r];
+  if (lane == 0) piv[col] = use ? (sgn > 0.f ? (int)arg + 1 : -((int)arg + 1)) : 0;
+}
+
+// C = A . Bm, plus sign Apiv[:, p] for the columns with a pivot (piv may be
+// null).
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
           const float* __restrict__ Bm, uint64_t ldb, uint32_t ncols,
           float* __restrict__ C, uint64_t ldc, uint32_t Kp, uint32_t Np,
-          uint32_t tmem_cols, int accumulate, int* __restrict__ err) {
+          uint32_t tmem_cols, int accumulate, const float* __restrict__ Apiv,
+          const int* __restrict__ piv, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
   __shared__ int stop;
   const TcLayout L(Kp, Np);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const uint32_t kq = Kp / 4;  // 16-byte K groups per row
+  const uint32_t kq = Kp / 8;  // 16-byte K groups (8 BF16) per row
   const uint32_t ntask = kTcRows * kq;
 
   if (wid == 0) {
@@ -152,28 +216,29 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   // B operand (N x K, K-major): row n of it is column n of Bm.
   for (uint32_t t = tid; t < Np * kq; t += kTcThreads) {
     const uint32_t n = t / kq, kg = t % kq;
-    float x[4];
+    float x[8];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t k = kg * 4 + j;
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t k = kg * 8 + j;
       x[j] = (n < ncols && k < K) ? Bm[(uint64_t)n * ldb + k] : 0.f;
     }
-    uint4 hi, lo;
-    split4(x, hi, lo);
-    *reinterpret_cast<uint4*>(smem + L.bhi + core_off(n, kg, kq)) = hi;
-    *reinterpret_cast<uint4*>(smem + L.blo + core_off(n, kg, kq)) = lo;
+    uint4 p[3];
+    split8(x, p);
+#pragma unroll
+    for (int part = 0; part < 3; ++part)
+      *reinterpret_cast<uint4*>(smem + L.b[part] + core_off(n, kg, kq)) = p[part];
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = idesc_tf32(kTcRows, Np);
+  const uint32_t idesc = idesc_bf16(kTcRows, Np);
   const uint32_t sbo = kq * 128u;
   const uint32_t base = smem_u32(smem);
 
   // A tile values of one tile, in registers: task = (row group, k group, row
   // in group); 8 lanes read 8 consecutive rows of one column (32-byte runs).
-  float xa[kTcTasks][4];
+  float xa[kTcTasks][8];
   auto load_tile = [&](uint64_t row0) {
 #pragma unroll
     for (int i = 0; i < kTcTasks; ++i) {
@@ -181,8 +246,8 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
       const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
       const uint64_t gr = row0 + rg * 8 + rr;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint32_t k = kg * 4 + j;
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t k = kg * 8 + j;
         xa[i][j] = (t < ntask && gr < rows && k < K) ? A[(uint64_t)k * lda + gr] : 0.f;
       }
     }
@@ -199,10 +264,12 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
       const uint32_t t = tid + i * kTcThreads;
       if (t < ntask) {
         const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
-        uint4 hi, lo;
-        split4(xa[i], hi, lo);
-        *reinterpret_cast<uint4*>(smem + L.ahi + core_off(rg * 8 + rr, kg, kq)) = hi;
-        *reinterpret_cast<uint4*>(smem + L.alo + core_off(rg * 8 + rr, kg, kq)) = lo;
+        uint4 p[3];
+        split8(xa[i], p);
+#pragma unroll
+        for (int part = 0; part < 3; ++part)
+          *reinterpret_cast<uint4*>(smem + L.a[part] + core_off(rg * 8 + rr, kg, kq)) =
+              p[part];
       }
     }
     fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
@@ -210,15 +277,25 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     __syncthreads();
     if (tid == 0) {
       tc_fence_after();
-      for (uint32_t ks = 0; ks < Kp / 8; ++ks) {
-        const uint32_t off = ks * 256u;  // two 16-byte K groups per K=8 step
-        const uint64_t ah = smem_desc(base + L.ahi + off, 128u, sbo);
-        const uint64_t al = smem_desc(base + L.alo + off, 128u, sbo);
-        const uint64_t bh = smem_desc(base + L.bhi + off, 128u, sbo);
-        const uint64_t bl = smem_desc(base + L.blo + off, 128u, sbo);
-        mma_tf32(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, idesc, 1u);
-        mma_tf32(tmem, al, bh, idesc, 1u);
+      for (uint32_t ks = 0; ks < Kp / 16; ++ks) {
+        const uint32_t off = ks * 256u;  // two 16-byte K groups per K=16 step
+        uint64_t da[3], db[3];
+#pragma unroll
+        for (int part = 0; part < 3; ++part) {
+          da[part] = smem_desc(base + L.a[part] + off, 128u, sbo);
+          db[part] = smem_desc(base + L.b[part] + off, 128u, sbo);
+        }
+        // the small cross products first: x1y3 + x2y2 + x3y1 + x1y2 + x2y1
+        mma_bf16(tmem, da[0], db[2], idesc, ks > 0 ? 1u : 0u);
+        mma_bf16(tmem, da[1], db[1], idesc, 1u);
+        mma_bf16(tmem, da[2], db[0], idesc, 1u);
+        mma_bf16(tmem, da[0], db[1], idesc, 1u);
+        mma_bf16(tmem, da[1], db[0], idesc, 1u);
+      }
+      for (uint32_t ks = 0; ks < Kp / 16; ++ks) {  // then x1y1
+        const uint32_t off = ks * 256u;
+        mma_bf16(tmem, smem_desc(base + L.a[0] + off, 128u, sbo),
+                 smem_desc(base + L.b[0] + off, 128u, sbo), idesc, 1u);
       }
       mma_commit(bar);
     }
@@ -243,8 +320,16 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           if (c0 + j < ncols) {
+            float val = v[j];
+            if (piv) {  // the pivot column, added in FP32
+              const int pv = piv[c0 + j];
+              if (pv != 0) {
+                const float a = Apiv[(uint64_t)(pv > 0 ? pv - 1 : -pv - 1) * lda + gr];
+                val = pv > 0 ? val + a : val - a;
+              }
+            }
             float* cp = C + (uint64_t)(c0 + j) * ldc + gr;
-            *cp = accumulate ? *cp + v[j] : v[j];  // K chunks add in order
+            *cp = accumulate ? *cp + val : val;  // K chunks add in order
           }
         }
       }
@@ -270,14 +355,15 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
 
 bool gemm_tc_supported(uint32_t K, uint32_t ncols) {
   if (K == 0 || ncols == 0 || K > 112 || ncols > 256) return false;
-  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 31) & ~31u;
+  const uint32_t Kp = (K + 15) & ~15u, Np = (ncols + 31) & ~31u;
   return TcLayout(Kp, Np).total <= 227 * 1024;
 }
 
 static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                            const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
-                           uint64_t ldc, int accumulate, int* err, cudaStream_t s) {
-  const uint32_t Kp = (K + 7) & ~7u, Np = (ncols + 31) & ~31u;
+                           uint64_t ldc, int accumulate, const float* Apiv,
+                           const int* piv, int* err, cudaStream_t s) {
+  const uint32_t Kp = (K + 15) & ~15u, Np = (ncols + 31) & ~31u;
   uint32_t tcols = 32;
   while (tcols < Np) tcols <<= 1;
   // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM
@@ -286,7 +372,7 @@ static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t
   const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
   const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)num_sms());
   k_gemm_tc<<<grid, kTcThreads, smem, s>>>(A, lda, rows, K, Bm, ldb, ncols, C, ldc,
-                                           Kp, Np, tcols, accumulate, err);
+                                           Kp, Np, tcols, accumulate, Apiv, piv, err);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }
@@ -295,22 +381,27 @@ static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t
 // the 10M-cell solve's m = 200) run as K chunks of <= 112 and column chunks
 // of <= 128: each chunk's operands fit the 227 KB of shared memory, and the
 // K chunks of a column chunk add into C in chunk order (fixed, so the result
-// is the same on every run).
+// is the same on every run); the first K chunk adds the pivot columns.
 int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                    const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
-                   uint64_t ldc, int* err, cudaStream_t s) {
+                   uint64_t ldc, float* dwork, int* piv, int* err, cudaStream_t s) {
   if (rows == 0 || ncols == 0) return BGPU_OK;
   BGPU_REQUIRE(K >= 1 && ncols <= K && K <= kTcMaxK, BGPU_ERR_UNSUPPORTED,
                "tensor-core rotation needs 1 <= ncols <= K <= 1024");
+  BGPU_REQUIRE(dwork && piv, BGPU_ERR_INVALID, "tensor-core rotation needs its scratch");
+  k_rot_pivots<<<(unsigned)ceil_div((uint64_t)ncols * 32, 256), 256, 0, s>>>(
+      Bm, ldb, K, ncols, dwork, piv);
+  BGPU_CHECK_LAUNCH();
   if (gemm_tc_supported(K, ncols))
-    return launch_tc_chunk(A, lda, rows, K, Bm, ldb, ncols, C, ldc, 0, err, s);
+    return launch_tc_chunk(A, lda, rows, K, dwork, K, ncols, C, ldc, 0, A, piv, err, s);
   for (uint32_t n0 = 0; n0 < ncols; n0 += kTcChunkN) {
     const uint32_t nc = std::min(kTcChunkN, ncols - n0);
     for (uint32_t k0 = 0; k0 < K; k0 += kTcChunkK) {
       const uint32_t kk = std::min(kTcChunkK, K - k0);
       BGPU_TRY(launch_tc_chunk(A + (uint64_t)k0 * lda, lda, rows, kk,
-                               Bm + (uint64_t)n0 * ldb + k0, ldb, nc,
-                               C + (uint64_t)n0 * ldc, ldc, k0 > 0 ? 1 : 0, err, s));
+                               dwork + (uint64_t)n0 * K + k0, K, nc,
+                               C + (uint64_t)n0 * ldc, ldc, k0 > 0 ? 1 : 0, A,
+                               k0 == 0 ? piv + n0 : nullptr, err, s));
     }
   }
   return BGPU_OK;

@@ -162,9 +162,10 @@ typedef struct bgpu_solve_opts {
                                 2 = two passes always (CGS2). The V side
                                 follows the same rule.                          */
   uint32_t rotation_mode;    /* restart rotation of U: 0 = default (tensor
-                                cores), 1 = FP32 SIMT GEMM, 2 = tcgen05 3-pass
-                                TF32 split GEMM with FP32 accumulation (K /
-                                column chunks beyond 112 / 128)                  */
+                                cores), 1 = FP32 SIMT GEMM, 2 = tcgen05 3 x
+                                BF16 split GEMM with FP32 accumulation and the
+                                dominant column of each rotation column added
+                                in FP32 (K / column chunks beyond 112 / 128)   */
   volatile int32_t* cancel;  /* host flag polled between Lanczos steps; may be
                                 NULL (replaces PyErr_CheckSignals, pca.pyx:1173) */
   int use_graphs;            /* reserved for CUDA-graph replay of the Lanczos
@@ -237,8 +238,11 @@ BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_hos
  * reference's matmul_nn_f_out at pca.pyx:578-616, U <- U . Ub[:, :kc]).
  * Device pointers, all column-major: A rows x K (lda), Bm K x >= ncols (ldb),
  * C rows x ncols (ldc). mode 1: FP32 SIMT; mode 2: tensor cores (tcgen05,
- * 3-pass TF32 split, FP32 accumulation; K > 112 or ncols > 128 run as
- * chunks whose K parts add in a fixed order). Synchronous. */
+ * 3 x BF16 split operands, six cross products accumulated in FP32; a column
+ * of Bm dominated by one entry (|entry| >= 1/2) is applied as that column of
+ * A, added in FP32, plus the tensor-core product with the rest; K > 112 or
+ * ncols > 128 run as chunks whose K parts add in a fixed order).
+ * Synchronous. */
 BGPU_API int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
                                uint32_t K, const float* Bm, uint64_t ldb,
                                uint32_t ncols, float* C, uint64_t ldc, int mode,

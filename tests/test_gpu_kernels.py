@@ -217,15 +217,26 @@ def test_small_svd(cuda, m):
                                           (5000, 200, 199), (3000, 150, 129),
                                           (777, 256, 256), (1000, 113, 5)])
 def test_rotate_basis_tensor_cores(cuda, rows, K, ncols):
-    """U . Ub[:, :kc] on the tensor cores (3-pass TF32 split) against the SIMT
-    FP32 GEMM and an FP64 product: both within 2e-6 of the FP64 scale (the
-    chunked shapes add their K parts in FP32, in chunk order)."""
-    import torch
+    """U . Ub[:, :kc] on the tensor cores (3 x BF16 split, six cross products,
+    FP32 accumulation) against the SIMT FP32 GEMM and an FP64 product, for a
+    general orthogonal Ub (no dominated columns): both within 2e-6 of the
+    FP64 scale (the chunked shapes add their K parts in FP32, in chunk
+    order)."""
     rng = np.random.default_rng(rows + K + ncols)
     lda = rows + 64 - rows % 64
     A = np.zeros((K, lda), dtype=np.float32)  # column-major rows x K, ld = lda
     A[:, :rows] = rng.standard_normal((K, rows)).astype(np.float32) / np.sqrt(rows)
     Q, _ = np.linalg.qr(rng.standard_normal((K, K)))
+    out, ref, scale = _rotate_both(cuda, A, Q, rows, K, ncols)
+    for mode in (1, 2):
+        err = np.abs(out[mode] - ref) / scale
+        assert np.isfinite(out[mode]).all()
+        assert err.max() < 2e-6, (mode, err.max())
+
+
+def _rotate_both(cuda, A, Q, rows, K, ncols):
+    import torch
+    lda = A.shape[1]
     Bm = np.asfortranarray(Q.astype(np.float32))
     dA, dB = T(A.ravel(), cuda), T(Bm.ravel(order="F"), cuda)
     out = {}
@@ -233,13 +244,47 @@ def test_rotate_basis_tensor_cores(cuda, rows, K, ncols):
         dC = torch.full((ncols * lda,), np.nan, dtype=torch.float32, device=cuda)
         _lib.call("bgpu_rotate_basis", dA.data_ptr(), lda, rows, K, dB.data_ptr(), K,
                   ncols, dC.data_ptr(), lda, mode, None)
-        out[mode] = dC.cpu().numpy().reshape(ncols, lda)[:, :rows]
+        out[mode] = dC.cpu().numpy().reshape(ncols, lda)[:, :rows].astype(np.float64)
     ref = (A[:, :rows].T.astype(np.float64) @ Bm[:, :ncols].astype(np.float64)).T
     scale = (np.abs(A[:, :rows]).T.astype(np.float64) @ np.abs(Bm[:, :ncols])).T
+    return out, ref, scale
+
+
+@pytest.mark.parametrize("rows,K,ncols", [(20000, 100, 99), (20000, 100, 60),
+                                          (8000, 200, 150), (5000, 64, 64)])
+def test_rotate_basis_ritz_rotation_unbiased(cuda, rows, K, ncols):
+    """The restart's rotation of converged Ritz vectors: Ub is a signed,
+    partly permuted near-identity (each column dominated by one entry), and
+    one column is exactly a unit vector. The tensor core's FP32 accumulation
+    truncates toward zero; the pivoted delta form adds the dominant column in
+    FP32, so the rotated columns keep their norms: the signed relative error
+    stays at the FP32 GEMM's level (|bias| < 3e-8, where a plain tensor-core
+    product of these shapes measured 5e-7), the RMS error within 1.5x the FP32
+    GEMM's, and the unit-vector column is copied exactly."""
+    rng = np.random.default_rng(rows + K)
+    lda = rows + 64 - rows % 64
+    Q0, _ = np.linalg.qr(rng.standard_normal((rows, K)))
+    A = np.zeros((K, lda), dtype=np.float32)
+    A[:, :rows] = Q0.T.astype(np.float32)
+    Q, _ = np.linalg.qr(np.eye(K) + 1e-3 * rng.standard_normal((K, K)))
+    Q = Q * np.sign(np.diag(Q))[None, :]
+    Q[:, 1::3] *= -1.0                    # sign flips
+    perm = np.arange(K)
+    perm[[2, 5]] = perm[[5, 2]]           # two Ritz values swapped places
+    Q = Q[:, perm]
+    Q[:, 0] = 0.0
+    Q[3, 0] = -1.0                        # a deflated (exactly converged) vector
+    Q[:, K - 1] = np.linalg.qr(rng.standard_normal((K, 1)))[0][:, 0]  # a mixed column
+    out, ref, _ = _rotate_both(cuda, A, Q, rows, K, ncols)
+    stats = {}
     for mode in (1, 2):
-        err = np.abs(out[mode] - ref) / scale
-        assert np.isfinite(out[mode]).all()
-        assert err.max() < 2e-6, (mode, err.max())
+        err = out[mode] - ref
+        bias = float(np.sum(err * np.sign(ref)) / np.sum(np.abs(ref)))
+        rms = float(np.sqrt(np.mean(err ** 2) / np.mean(ref ** 2)))
+        stats[mode] = (bias, rms)
+    assert abs(stats[2][0]) < 3e-8, stats
+    assert stats[2][1] <= 1.5 * stats[1][1] + 1e-8, stats
+    np.testing.assert_array_equal(out[2][0], -A[3, :rows].astype(np.float64))
 
 
 def test_row_order_does_not_change_products(cuda, monkeypatch):
