@@ -78,6 +78,8 @@ def parse():
                     help="skip the FP64 accuracy report of the CPU-baseline leg")
     ap.add_argument("--accuracy", action="store_true",
                     help="FP64 accuracy report even with --no-cpu-baseline")
+    ap.add_argument("--svd-mode", type=int, default=0,
+                    help="restart SVD: 0 default (merge), 1 FP64 Jacobi, 2 FP32 Jacobi + Newton")
     ap.add_argument("--rotation-mode", type=int, default=0,
                     help="restart rotation of U: 0 default, 1 FP32 SIMT, 2 tensor cores")
     ap.add_argument("--reorth-passes", default="auto",
@@ -382,7 +384,7 @@ def run_ours(args):
     pcs_dev = torch.empty((n, k), dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
         r = M.solve(k, m, reorth_passes=args.reorth_passes,
-                    rotation_mode=args.rotation_mode, PCs=pcs_dev,
+                    rotation_mode=args.rotation_mode, svd_mode=args.svd_mode, PCs=pcs_dev,
                     stream=stream)
     barrier()
     torch.cuda.synchronize()
@@ -393,7 +395,7 @@ def run_ours(args):
         start.record(stream)
         for _ in range(args.steps):
             r = M.solve(k, m, reorth_passes=args.reorth_passes,
-                        rotation_mode=args.rotation_mode, PCs=pcs_dev,
+                        rotation_mode=args.rotation_mode, svd_mode=args.svd_mode, PCs=pcs_dev,
                         profile=True, stream=stream)
             infos.append(r.info)
         stop.record(stream)
@@ -427,7 +429,7 @@ def run_ours(args):
                           norm="logCP10k", inv_size_factors=np_views[3],
                           stream=stream)
         Me.solve(k, m, reorth_passes=args.reorth_passes,
-                 rotation_mode=args.rotation_mode, PCs=np_views[4],
+                 rotation_mode=args.rotation_mode, svd_mode=args.svd_mode, PCs=np_views[4],
                  stream=stream)
         Me.close()
     torch.cuda.synchronize()

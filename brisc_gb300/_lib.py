@@ -51,7 +51,7 @@ class SolveOpts(C.Structure):
         ("cancel", C.c_void_p),
         ("use_graphs", C.c_int),
         ("profile", C.c_int),
-        ("svd_fp64", C.c_int),
+        ("svd_mode", C.c_uint32),
     ]
 
 

@@ -163,9 +163,11 @@ struct Solver {
 
   Buf U, Unew, V, Vnew, y0, y1, part, coef, zpart, zvec, rem, sd, Bf, Ub, Sb,
       Vbt, oaw, svdwork, scal, smax, B, st, sdpart, svdinfo, ub_last,
-      sb64, ratios, rotd, rotpiv,
+      sb64, ratios, rotd, rotpiv, tailw, mergew,
       derr, taken, ticket;
-  bool svd64 = false;  // FP64 Jacobi when opts.svd_fp64
+  uint32_t svd_mode = 0;     // opts.svd_mode
+  bool svd64 = false;        // full FP64 Jacobi (svd_mode 1)
+  uint32_t merged_svds = 0;  // restarts solved by the secular merge
   int rot_mode = 0;    // 1 = SIMT FP32 rotation, 2 = tensor-core 3 x BF16
   bool trace = false;  // BGPU_TRACE=1: one stderr line per restart
   HostStatus hst;
@@ -255,6 +257,10 @@ struct Solver {
     BGPU_TRY(balloc(Vbt, (size_t)m * (m + 1) * 4, true, s));
     BGPU_TRY(balloc(rotd, (size_t)m * m * 4, false, s));  // tensor-core rotation scratch
     BGPU_TRY(balloc(rotpiv, (size_t)m * 4, false, s));
+    if (svd_mode == 0) {  // secular-merge workspaces
+      BGPU_TRY(balloc(tailw, tail_work_bytes(m), false, s));
+      BGPU_TRY(balloc(mergew, merge_work_bytes(m), false, s));
+    }
     BGPU_TRY(balloc(oaw, svd_refine_doubles(m) * 8, true, s));
     if (jacobi_smem_bytes(m, svd64) > 220 * 1024)
       BGPU_TRY(balloc(svdwork, jacobi_global_bytes(m, svd64), true, s));
@@ -413,7 +419,9 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
   Solver S(X, o, s);
   S.profile = o.profile != 0;
   {
-    S.svd64 = o.svd_fp64 != 0;
+    BGPU_REQUIRE(o.svd_mode <= 2, BGPU_ERR_INVALID, "svd_mode must be 0, 1 or 2");
+    S.svd_mode = o.svd_mode;
+    S.svd64 = o.svd_mode == 1;
     BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
     // subspaces beyond one shared-memory staging run as K / column chunks
     const bool tc_ok = o.subspace_size <= 1024;
@@ -451,7 +459,17 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     }
     ++restarts;
     BGPU_TRY(S.ev_begin(2));
-    if (S.svd64) {
+    if (S.svd_mode == 0 && kc >= 1) {
+      // B = restart arrow + the cycle's Lanczos rows: the tail's SVD (t = m -
+      // kc rows) and an FP64 secular-equation merge instead of a full SVD
+      BGPU_TRY(launch_svd_merge(S.B.as<double>(), m, kc, S.Ub.as<float>(),
+                                S.Sb.as<float>(), S.Vbt.as<float>(),
+                                S.ub_last.as<double>(), S.sb64.as<double>(), S.tailw.p,
+                                S.mergew.p, S.oaw.as<double>(), S.svdwork.p,
+                                kRefineSteps, s));
+      S.launches += 7 + (m - kc > kMergeFp64TailMax ? 1 + 4 * kRefineSteps + 4 : 0);
+      ++S.merged_svds;
+    } else if (S.svd_mode == 1) {
       BGPU_TRY(launch_jacobi_svd(nullptr, S.B.as<double>(), m, S.Ub.as<float>(),
                                  S.Sb.as<float>(), S.Vbt.as<float>(),
                                  S.ub_last.as<double>(), S.sb64.as<double>(),

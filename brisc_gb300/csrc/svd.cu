@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(1024)
 k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
          float* __restrict__ Sb, float* __restrict__ Vbt,
          double* __restrict__ ub_last, double* __restrict__ sb64,
-         T* __restrict__ gwork, int use_smem, int max_sweeps, T thresh,
-         int* __restrict__ info) {
+         double* __restrict__ ub64, T* __restrict__ gwork, int use_smem,
+         int max_sweeps, T thresh, int* __restrict__ info) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int rotated;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -225,7 +225,10 @@ k_jacobi(const T* __restrict__ Bin, uint32_t m, float* __restrict__ Ub,
       if (sb64) sb64[rank] = (double)si;
       if (ub_last) ub_last[rank] = (double)ji[m - 1];
     }
-    for (uint32_t r = lane; r < m; r += 32) Ub[r + (uint64_t)rank * m] = (float)ji[r];
+    for (uint32_t r = lane; r < m; r += 32) {
+      Ub[r + (uint64_t)rank * m] = (float)ji[r];
+      if (ub64) ub64[r + (uint64_t)rank * m] = (double)ji[r];
+    }
     const T* ai = A + (uint64_t)i * lp;
     const T inv = si > T(0) ? T(1) / si : T(0);
     for (int r = lane; r < la; r += 32)
@@ -315,53 +318,64 @@ __global__ void k_f2d(const float* __restrict__ a, uint64_t n, double* __restric
 // which converges quadratically; three steps take FP32-accurate factors to
 // FP64 accuracy. Then sigma_i = sqrt(lam_i) and Vbt's rows are (B^T U)_i /
 // sigma_i.
-__global__ void k_oa_w(const double* __restrict__ B, const double* __restrict__ U,
-                       uint32_t m, double* __restrict__ W) {
-  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (t >= (uint64_t)(m + 1) * m) return;
-  const uint32_t r = (uint32_t)(t % (m + 1)), i = (uint32_t)(t / (m + 1));
-  const double* b = B + (uint64_t)r * m;  // row r of B^T = column r of B
-  const double* u = U + (uint64_t)i * m;
+// Warp-per-output dot products: lanes stride the summed index (coalesced,
+// contiguous columns), a fixed xor tree closes the sum.
+__device__ __forceinline__ double warp_dot64(const double* __restrict__ a,
+                                             const double* __restrict__ b,
+                                             uint32_t len, int lane) {
   double acc = 0.0;
-  for (uint32_t c = 0; c < m; ++c) acc = fma(b[c], u[c], acc);
-  W[r + (uint64_t)i * (m + 1)] = acc;
+  for (uint32_t c = lane; c < len; c += 32) acc = fma(a[c], b[c], acc);
+  return warp_sum_t(acc);
 }
 
-__global__ void k_oa_sr(const double* __restrict__ W, const double* __restrict__ U,
-                        uint32_t m, double* __restrict__ S, double* __restrict__ R) {
+// W = B^T U: W[r, i] = column r of B . column i of U ((m+1) x m outputs).
+__global__ void __launch_bounds__(256)
+k_oa_w(const double* __restrict__ B, const double* __restrict__ U, uint32_t m,
+       double* __restrict__ W) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= (uint64_t)(m + 1) * m) return;
+  const uint32_t r = (uint32_t)(w % (m + 1)), i = (uint32_t)(w / (m + 1));
+  const double v = warp_dot64(B + (uint64_t)r * m, U + (uint64_t)i * m, m, lane);
+  if (lane == 0) W[r + (uint64_t)i * (m + 1)] = v;
+}
+
+// S = W^T W and R = I - U^T U (m x m outputs, one warp each).
+__global__ void __launch_bounds__(256)
+k_oa_sr(const double* __restrict__ W, const double* __restrict__ U, uint32_t m,
+        double* __restrict__ S, double* __restrict__ R) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= (uint64_t)m * m) return;
+  const uint32_t i = (uint32_t)(w % m), j = (uint32_t)(w / m);
+  const double s = warp_dot64(W + (uint64_t)i * (m + 1), W + (uint64_t)j * (m + 1),
+                              m + 1, lane);
+  const double q = warp_dot64(U + (uint64_t)i * m, U + (uint64_t)j * m, m, lane);
+  if (lane == 0) {
+    S[w] = s;
+    R[w] = (i == j ? 1.0 : 0.0) - q;
+  }
+}
+
+// lam_i = S_ii / (1 - R_ii) and the Newton correction E (m x m outputs,
+// one thread each; every thread recomputes the two lam it needs).
+__global__ void __launch_bounds__(256)
+k_oa_e(const double* __restrict__ S, const double* __restrict__ R, uint32_t m,
+       double* __restrict__ lam, double* __restrict__ E) {
   const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (t >= (uint64_t)m * m) return;
   const uint32_t i = (uint32_t)(t % m), j = (uint32_t)(t / m);
-  const double* wi = W + (uint64_t)i * (m + 1);
-  const double* wj = W + (uint64_t)j * (m + 1);
-  double s = 0.0;
-  for (uint32_t r = 0; r <= m; ++r) s = fma(wi[r], wj[r], s);
-  const double* ui = U + (uint64_t)i * m;
-  const double* uj = U + (uint64_t)j * m;
-  double q = 0.0;
-  for (uint32_t c = 0; c < m; ++c) q = fma(ui[c], uj[c], q);
-  S[t] = s;
-  R[t] = (i == j ? 1.0 : 0.0) - q;
-}
-
-__global__ void __launch_bounds__(1024)
-k_oa_e(const double* __restrict__ S, const double* __restrict__ R, uint32_t m,
-       double* __restrict__ lam, double* __restrict__ E) {
-  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-    const uint64_t d = (uint64_t)i * m + i;
-    lam[i] = S[d] / (1.0 - R[d]);
+  const uint64_t di = (uint64_t)i * m + i, dj = (uint64_t)j * m + j;
+  const double li = S[di] / (1.0 - R[di]);
+  const double lj = S[dj] / (1.0 - R[dj]);
+  if (i == j) lam[i] = li;
+  double e = 0.5 * R[t];
+  if (i != j) {
+    const double num = S[t] + lj * R[t];
+    const double den = lj - li;
+    if (fabs(num) < 0.25 * fabs(den)) e = num / den;
   }
-  __syncthreads();
-  for (uint64_t t = threadIdx.x; t < (uint64_t)m * m; t += blockDim.x) {
-    const uint32_t i = (uint32_t)(t % m), j = (uint32_t)(t / m);
-    double e = 0.5 * R[t];
-    if (i != j) {
-      const double num = S[t] + lam[j] * R[t];
-      const double den = lam[j] - lam[i];
-      if (fabs(num) < 0.25 * fabs(den)) e = num / den;
-    }
-    E[t] = e;
-  }
+  E[t] = e;
 }
 
 __global__ void k_oa_u(const double* __restrict__ U, const double* __restrict__ E,
@@ -375,25 +389,27 @@ __global__ void k_oa_u(const double* __restrict__ U, const double* __restrict__ 
   Un[t] = acc;
 }
 
-__global__ void k_oa_out(const double* __restrict__ B, const double* __restrict__ U,
-                         const double* __restrict__ lam, uint32_t m,
-                         float* __restrict__ Ub, float* __restrict__ Sb,
-                         float* __restrict__ Vbt, double* __restrict__ ub_last,
-                         double* __restrict__ sb64) {
-  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (t >= (uint64_t)(m + 1) * m) return;
-  const uint32_t i = (uint32_t)(t % m), r = (uint32_t)(t / m);  // Vbt[i + r m]
+// Outputs: Vbt[i, r] = (B^T U)[r, i] / sigma_i (one warp each), Ub, Sb and
+// the FP64 last row of Ub and singular values.
+__global__ void __launch_bounds__(256)
+k_oa_out(const double* __restrict__ B, const double* __restrict__ U,
+         const double* __restrict__ lam, uint32_t m, float* __restrict__ Ub,
+         float* __restrict__ Sb, float* __restrict__ Vbt, double* __restrict__ ub_last,
+         double* __restrict__ sb64) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= (uint64_t)(m + 1) * m) return;
+  const uint32_t i = (uint32_t)(w % m), r = (uint32_t)(w / m);
   const double sig = sqrt(fmax(lam[i], 0.0));
-  const double* b = B + (uint64_t)r * m;
-  const double* u = U + (uint64_t)i * m;
-  double acc = 0.0;
-  for (uint32_t c = 0; c < m; ++c) acc = fma(b[c], u[c], acc);
-  Vbt[t] = sig > 0.0 ? (float)(acc / sig) : 0.f;
-  if (r < m) Ub[(uint64_t)r + (uint64_t)i * m] = (float)U[(uint64_t)r + (uint64_t)i * m];
-  if (r == 0) {
-    Sb[i] = (float)sig;
-    sb64[i] = sig;
-    ub_last[i] = U[(uint64_t)(m - 1) + (uint64_t)i * m];
+  const double v = warp_dot64(B + (uint64_t)r * m, U + (uint64_t)i * m, m, lane);
+  if (lane == 0) {
+    Vbt[w] = sig > 0.0 ? (float)(v / sig) : 0.f;
+    if (r < m) Ub[(uint64_t)r + (uint64_t)i * m] = (float)U[(uint64_t)r + (uint64_t)i * m];
+    if (r == 0) {
+      Sb[i] = (float)sig;
+      sb64[i] = sig;
+      ub_last[i] = U[(uint64_t)(m - 1) + (uint64_t)i * m];
+    }
   }
 }
 
@@ -405,7 +421,7 @@ size_t svd_refine_doubles(uint32_t m) {
 
 int launch_svd_refine(const double* B, uint32_t m, float* Ub, float* Sb, float* Vbt,
                       double* ub_last, double* sb64, double* work, int steps,
-                      cudaStream_t s) {
+                      cudaStream_t s, double* u64_out) {
   const uint64_t mm = (uint64_t)m * m;
   double* U = work;
   double* Un = U + mm;
@@ -414,30 +430,34 @@ int launch_svd_refine(const double* B, uint32_t m, float* Ub, float* Sb, float* 
   double* E = R + mm;
   double* W = E + mm;
   double* lam = W + (uint64_t)(m + 1) * m;
-  const unsigned gw = (unsigned)ceil_div((uint64_t)(m + 1) * m, 128);
+  // warp-per-output kernels: 8 outputs per 256-thread block
+  const unsigned gw = (unsigned)ceil_div((uint64_t)(m + 1) * m, 8);
+  const unsigned gs = (unsigned)ceil_div(mm, 8);
+  const unsigned ge = (unsigned)ceil_div(mm, 256);
   const unsigned gm = (unsigned)ceil_div(mm, 128);
   k_f2d<<<(unsigned)ceil_div(mm, 256), 256, 0, s>>>(Ub, mm, U);
   BGPU_CHECK_LAUNCH();
   for (int it = 0; it < steps; ++it) {
-    k_oa_w<<<gw, 128, 0, s>>>(B, U, m, W);
+    k_oa_w<<<gw, 256, 0, s>>>(B, U, m, W);
     BGPU_CHECK_LAUNCH();
-    k_oa_sr<<<gm, 128, 0, s>>>(W, U, m, Sm, R);
+    k_oa_sr<<<gs, 256, 0, s>>>(W, U, m, Sm, R);
     BGPU_CHECK_LAUNCH();
-    k_oa_e<<<1, 1024, 0, s>>>(Sm, R, m, lam, E);
+    k_oa_e<<<ge, 256, 0, s>>>(Sm, R, m, lam, E);
     BGPU_CHECK_LAUNCH();
     k_oa_u<<<gm, 128, 0, s>>>(U, E, m, Un);
     BGPU_CHECK_LAUNCH();
     std::swap(U, Un);
   }
   // the eigenvalues of the refined U: one more S diagonal
-  k_oa_w<<<gw, 128, 0, s>>>(B, U, m, W);
+  k_oa_w<<<gw, 256, 0, s>>>(B, U, m, W);
   BGPU_CHECK_LAUNCH();
-  k_oa_sr<<<gm, 128, 0, s>>>(W, U, m, Sm, R);
+  k_oa_sr<<<gs, 256, 0, s>>>(W, U, m, Sm, R);
   BGPU_CHECK_LAUNCH();
-  k_oa_e<<<1, 1024, 0, s>>>(Sm, R, m, lam, E);
+  k_oa_e<<<ge, 256, 0, s>>>(Sm, R, m, lam, E);
   BGPU_CHECK_LAUNCH();
-  k_oa_out<<<gw, 128, 0, s>>>(B, U, lam, m, Ub, Sb, Vbt, ub_last, sb64);
+  k_oa_out<<<gw, 256, 0, s>>>(B, U, lam, m, Ub, Sb, Vbt, ub_last, sb64);
   BGPU_CHECK_LAUNCH();
+  if (u64_out) BGPU_CUDA(cudaMemcpyAsync(u64_out, U, mm * 8, cudaMemcpyDeviceToDevice, s));
   return BGPU_OK;
 }
 
@@ -463,7 +483,7 @@ float jacobi_threshold(uint32_t m) {
 
 int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
                       float* Sb, float* Vbt, double* ub_last, double* sb64,
-                      void* gwork, int* info, cudaStream_t s) {
+                      void* gwork, int* info, cudaStream_t s, double* ub64) {
   const bool fp64 = Bd != nullptr;
   const size_t smem = jacobi_smem_bytes(m, fp64);
   const bool use_smem = smem <= 220 * 1024;
@@ -473,13 +493,13 @@ int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
     if (use_smem && smem > 48 * 1024)
       BGPU_CUDA(allow_max_smem(k_jacobi<double>));
     k_jacobi<double><<<1, 1024, use_smem ? smem : 0, s>>>(
-        Bd, m, Ub, Sb, Vbt, ub_last, sb64, (double*)gwork, use_smem ? 1 : 0, 40,
+        Bd, m, Ub, Sb, Vbt, ub_last, sb64, ub64, (double*)gwork, use_smem ? 1 : 0, 40,
         1e-13, info);
   } else {
     if (use_smem && smem > 48 * 1024)
       BGPU_CUDA(allow_max_smem(k_jacobi<float>));
     k_jacobi<float><<<1, 1024, use_smem ? smem : 0, s>>>(
-        Bf, m, Ub, Sb, Vbt, ub_last, sb64, (float*)gwork, use_smem ? 1 : 0, 40,
+        Bf, m, Ub, Sb, Vbt, ub_last, sb64, ub64, (float*)gwork, use_smem ? 1 : 0, 40,
         jacobi_threshold(m), info);
   }
   BGPU_CHECK_LAUNCH();

@@ -25,7 +25,7 @@ float jacobi_threshold(uint32_t m);
 size_t svd_refine_doubles(uint32_t m);
 int launch_svd_refine(const double* B, uint32_t m, float* Ub, float* Sb, float* Vbt,
                       double* ub_last, double* sb64, double* work, int steps,
-                      cudaStream_t s);
+                      cudaStream_t s, double* u64_out = nullptr);
 int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s);
 
 // One-sided Jacobi SVD of B (m x (m+1), column-major), in FP64 when Bd is
@@ -33,10 +33,10 @@ int launch_float_to_double(const float* a, uint64_t n, double* b, cudaStream_t s
 // (m x (m+1)), column-major; optionally the FP64 last row of Ub (ub_last, m)
 // and FP64 singular values (sb64, m). gwork: jacobi_global_bytes(m, fp64)
 // bytes when the matrices do not fit in shared memory; info (2 ints: sweeps,
-// converged) may be null.
+// converged) may be null; ub64 (may be null) receives Ub in FP64.
 int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
                       float* Sb, float* Vbt, double* ub_last, double* sb64,
-                      void* gwork, int* info, cudaStream_t s);
+                      void* gwork, int* info, cudaStream_t s, double* ub64 = nullptr);
 
 // Normalises rem, updates Smax, counts converged Ritz values, picks the next
 // k_current and (when not converged) rebuilds B as diag(Sb) plus the residual
@@ -48,5 +48,25 @@ int launch_restart_check(const float* Ub, const float* Sb, const double* ub_last
                          uint32_t g, float tol, float* smax, uint32_t kc,
                          double* B, RestartStatus* st, float* ratios,
                          cudaStream_t s);
+
+// Restart SVD by a secular-equation merge (svd_merge.cu), for B as rebuilt
+// by the restart (diag(s) in columns < kc, residual column kc) plus the t =
+// m - kc Lanczos rows of the cycle: the tail's SVD (size t), then the
+// eigenpairs of diag(s^2, mu) + z z^T in FP64. Same outputs as
+// launch_jacobi_svd + launch_svd_refine. Workspaces: tailw tail_work_bytes(m),
+// mergew merge_work_bytes(m), refine_work svd_refine_doubles(m) doubles,
+// jacobi_gwork as for launch_jacobi_svd at size m (may be null where that
+// needs none).
+constexpr uint32_t kMergeFp64TailMax = 12;  // tails up to this size: FP64 Jacobi
+struct MergeWork {
+  double *ds, *zs, *dn, *zn, *tau, *zhat, *lam, *rot_c, *rot_s, *znorm2;
+  int *src, *defl, *ndpos, *defpos, *rot_p, *rot_q, *korig, *order, *state;
+};
+size_t tail_work_bytes(uint32_t m);
+size_t merge_work_bytes(uint32_t m);
+int launch_svd_merge(const double* B, uint32_t m, uint32_t kc, float* Ub, float* Sb,
+                     float* Vbt, double* ub_last, double* sb64, void* tailw,
+                     void* mergew, double* refine_work, void* jacobi_gwork,
+                     int refine_steps, cudaStream_t s);
 
 }  // namespace bgpu

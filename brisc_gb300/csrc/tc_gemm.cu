@@ -197,6 +197,7 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
   __shared__ int stop;
+  __shared__ int spiv[kTcChunkN];  // pivot of each output column (0: none)
   const TcLayout L(Kp, Np);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const uint32_t kq = Kp / 8;  // 16-byte K groups (8 BF16) per row
@@ -213,6 +214,8 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     fence_mbar_init();
     stop = 0;
   }
+  for (uint32_t c = tid; c < kTcChunkN; c += kTcThreads)
+    spiv[c] = (piv && c < ncols) ? piv[c] : 0;
   // B operand (N x K, K-major): row n of it is column n of Bm.
   for (uint32_t t = tid; t < Np * kq; t += kTcThreads) {
     const uint32_t n = t / kq, kg = t % kq;
@@ -301,6 +304,25 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     }
     // the next tile's loads fly while the MMAs run and the accumulator drains
     if (tile + gridDim.x < ntiles) load_tile((tile + gridDim.x) * kTcRows);
+    // Epilogue mapping: warp w reads TMEM lanes 32*(w%4).. (tile rows) and
+    // the columns of quarter w/4 (<= 32 columns); lane = row. The pivot
+    // columns' FP32 values of this thread's row (L2-resident: the tile was
+    // just read) are fetched now, all in flight at once, signed.
+    const uint32_t q = wid & 3u, h = wid >> 2;
+    const uint32_t quarter = Np / 4;
+    const uint64_t gr = row0 + q * 32 + lane;
+    float pa[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const uint32_t c = h * quarter + j;
+      const int pv = (j < (int)quarter && c < ncols) ? spiv[c] : 0;
+      float a = 0.f;
+      if (pv != 0 && gr < rows) {
+        a = Apiv[(uint64_t)(pv > 0 ? pv - 1 : -pv - 1) * lda + gr];
+        if (pv < 0) a = -a;
+      }
+      pa[j] = a;
+    }
     const bool ok = mbar_wait(bar, phase, err);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) stop = 1;
@@ -308,26 +330,17 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     }
     phase ^= 1u;
     tc_fence_after();
-    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (tile rows) and the
-    // columns of quarter w/4; lane = row.
-    const uint32_t q = wid & 3u, h = wid >> 2;
-    const uint32_t quarter = Np / 4;
-    const uint64_t gr = row0 + q * 32 + lane;
-    for (uint32_t c0 = h * quarter; c0 < (h + 1) * quarter; c0 += 8) {
+#pragma unroll
+    for (uint32_t g8 = 0; g8 < 4; ++g8) {
+      const uint32_t c0 = h * quarter + g8 * 8;
+      if (g8 * 8 >= quarter) break;
       float v[8];
       tmem_ld8(tmem + ((q * 32u) << 16) + c0, v);
       if (gr < rows) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           if (c0 + j < ncols) {
-            float val = v[j];
-            if (piv) {  // the pivot column, added in FP32
-              const int pv = piv[c0 + j];
-              if (pv != 0) {
-                const float a = Apiv[(uint64_t)(pv > 0 ? pv - 1 : -pv - 1) * lda + gr];
-                val = pv > 0 ? val + a : val - a;
-              }
-            }
+            const float val = v[j] + pa[g8 * 8 + j];  // pivot column, FP32 add
             float* cp = C + (uint64_t)(c0 + j) * ldc + gr;
             *cp = accumulate ? *cp + val : val;  // K chunks add in order
           }

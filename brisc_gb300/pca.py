@@ -227,7 +227,7 @@ class DeviceMatrix:
               reorth_passes: int | str = "auto",
               rotation_mode: int = 0, loadings: bool = False, PCs=None,
               use_graphs: bool = False, profile: bool = False,
-              svd_fp64: bool = False, stream=None) -> SolveResult:
+              svd_mode: int = 0, stream=None) -> SolveResult:
         o = L.SolveOpts()
         L.lib().bgpu_solve_opts_default(C.byref(o))
         o.k, o.subspace_size = int(num_PCs), int(subspace_size)
@@ -236,7 +236,7 @@ class DeviceMatrix:
         o.reorth_passes = reorth_code(reorth_passes)
         o.rotation_mode = int(rotation_mode)
         o.use_graphs, o.profile = int(use_graphs), int(profile)
-        o.svd_fp64 = int(svd_fp64)
+        o.svd_mode = int(svd_mode)
         on_dev = PCs is not None and not isinstance(PCs, np.ndarray)
         if PCs is None:
             PCs = np.empty((self.num_cells, num_PCs), dtype=np.float32)

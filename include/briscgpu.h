@@ -172,8 +172,16 @@ typedef struct bgpu_solve_opts {
                                 steps; accepted and currently ignored            */
   int profile;               /* time the sparse products and the small SVD with
                                 CUDA events (fills the *_seconds fields)         */
-  int svd_fp64;              /* small SVD in FP64 (1) or FP32 (0); B and the
-                                convergence test are FP64 either way            */
+  uint32_t svd_mode;         /* restart SVD of B (replaces sgesdd, pca.pyx:1178):
+                                0 = default: at the first restart FP32 Jacobi
+                                + FP64 Newton refinement of the whole B; at
+                                every later restart an FP64 secular-equation
+                                merge of the restart arrow with the cycle's
+                                Lanczos rows (only those t = m - kc rows get a
+                                small SVD of their own); 1 = FP64 Jacobi of
+                                the whole B every restart; 2 = FP32 Jacobi +
+                                FP64 Newton of the whole B every restart. B
+                                and the convergence test are FP64 always.    */
 } bgpu_solve_opts;
 
 typedef struct bgpu_solve_info {

@@ -98,7 +98,7 @@ def test_bit_identical_runs(cuda, golden):
                          [("auto", 0), (1, 0), (2, 0), (2, 1), (2, 2)])
 def test_reorth_passes_both_meet_gates(cuda, golden, passes, rotation):
     """Every Gram-Schmidt mode (adaptive, one pass, CGS2) and both restart
-    rotations (SIMT FP32 and the tensor-core 3-pass TF32 split) meet the FP64
+    rotations (SIMT FP32 and the tensor-core 3 x BF16 split) meet the FP64
     gates."""
     z = golden("irlba")
     X, n, g, k, m = _case(z, "clustered_b")
@@ -112,6 +112,32 @@ def test_reorth_passes_both_meet_gates(cuda, golden, passes, rotation):
     # loadings are the right singular vectors: A^T u = s v
     assert dense.max_angle(r.loadings, Vt.T[:, :k]) < 1e-3
     assert dense.residuals(X, r.PCs).max() < 1e-3
+
+
+@pytest.mark.parametrize("name", ["clustered_a", "clustered_b", "flat"])
+def test_restart_svd_modes_agree(cuda, golden, name):
+    """The restart SVD by secular-equation merge (default), the FP64 Jacobi of
+    the whole B and the FP32 Jacobi + FP64 Newton of the whole B all give
+    the FP64 singular values within 1e-4, PCs within the angle gate of each
+    other on the gapped fixtures, and restart counts within one of each
+    other (all three are FP64-accurate, so they converge alike)."""
+    z = golden("irlba")
+    X, n, g, k, m = _case(z, name)
+    S, U, Vt = dense.top_svd(X, k + 2)
+    out = {}
+    for mode in (0, 1, 2):
+        M = DeviceMatrix(X.indptr, X.indices, X.data, n, g)
+        r = M.solve(k, m, svd_mode=mode)
+        M.close()
+        assert r.converged, mode
+        assert dense.rel_sv_error(r.PCs, S).max() < 1e-4, mode
+        out[mode] = r
+    for mode in (1, 2):
+        assert abs(out[mode].info["restarts"] - out[0].info["restarts"]) <= 1
+        np.testing.assert_allclose(out[mode].singular_values, out[0].singular_values,
+                                   rtol=1e-5)
+        if name != "flat":
+            assert dense.max_angle(out[mode].PCs, out[0].PCs) < 1e-3
 
 
 def test_flat_spectrum_singular_values(cuda, golden):
@@ -224,10 +250,9 @@ def test_cancel_flag(cuda, golden):
 
 def test_large_solve_meets_fp64_gate(cuda):
     """200k cells x 2000 genes at 5% density (the 1M workload's generator),
-    default settings (FP32 small SVD with the FP64 polish, adaptive
-    Gram-Schmidt, tensor-core rotation): relative singular-value error <= 1e-4
-    against the FP64
-    Gram-matrix oracle, and the solve converges."""
+    default settings (secular-merge restart SVD, adaptive Gram-Schmidt,
+    tensor-core rotation): relative singular-value error <= 1e-4 against the
+    FP64 Gram-matrix oracle, and the solve converges."""
     from synth import nb_counts
     c = nb_counts(200_000, 2000, seed=0, density=0.05)
     M = DeviceMatrix(c.indptr.astype(np.int32), c.indices, c.data, c.num_cells, 2000,
