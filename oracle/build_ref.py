@@ -6,7 +6,8 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 
 1. ``cythonize`` (needs Cython and the reference checkout): translate the
    reference modules on the path -- ``brisc/cyutils.pyx``, ``brisc/pca.pyx``,
-   ``brisc/normalize.pyx``, ``brisc/cysparse.pyx``, ``brisc/hvg.pyx`` -- plus the test harness
+   ``brisc/normalize.pyx``, ``brisc/cysparse.pyx``, ``brisc/hvg.pyx``,
+   ``brisc/kmeans.pyx``, ``brisc/knn.pyx`` -- plus the test harness
    ``oracle/ref_probe.pyx`` to C++ under ``oracle/_ref/gen/``. The sources are
    read where they lie; nothing is copied into the repository.
 2. ``compile`` (needs only g++, Python and numpy headers): build every
@@ -14,7 +15,10 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
    reference's own Linux flags (``setup.py:92-100`` of the reference:
    ``-Ofast -funroll-loops -std=c++17 -fopenmp`` plus the ``-march`` of the
    variant the reference would load on this CPU, ``setup.py:34-42`` and
-   ``brisc/utils.py:29-49``: the SVE build on Grace).
+   ``brisc/utils.py:29-49``: on aarch64 the SVE build only where numpy
+   reports SVE. The GPU host's Grace cores list no ``sve`` in
+   ``/proc/cpuinfo`` and numpy reports none there, so the reference itself
+   loads its plain ``armv8.2-a`` build on that host, and so does this recipe).
 
 Stage 2 runs on any machine that received ``oracle/_ref/gen`` (the C++ is
 architecture-neutral), so the aarch64 GPU host can rebuild the reference
@@ -38,10 +42,11 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 GEN = REF_OUT / "gen"
-MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg"]
+MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn"]
 # What the CPU baselines need (cysparse's 24 MB of C++ is only needed for the
 # transpose fixture and is skipped where compile time matters).
-BASELINE_MODULES = ["cyutils", "pca", "normalize", "hvg", "ref_probe"]
+BASELINE_MODULES = ["cyutils", "pca", "normalize", "hvg", "kmeans", "knn",
+                    "ref_probe"]
 DIRECTIVES = {"language_level": "3", "boundscheck": False,
               "wraparound": False, "cdivision": True,
               "initializedcheck": False, "warn.undeclared": False}
@@ -65,8 +70,8 @@ def march_flag() -> list[str]:
     """The -march of the variant the reference itself would load here: its
     setup.py:34-42 builds one per instruction-set level and its
     import_cython (brisc/utils.py:29-49) picks x86-64-v4 with AVX-512F, v3
-    with AVX2, else v2; on aarch64 the SVE build where the CPU has SVE (as
-    Grace does), else plain armv8.2-a."""
+    with AVX2, else v2; on aarch64 the SVE build where numpy reports SVE,
+    else plain armv8.2-a."""
     m = platform.machine().lower()
     try:
         from numpy._core._multiarray_umath import __cpu_features__ as cpu

@@ -57,11 +57,12 @@ def load(build: bool = True):
     if str(d) not in sys.path:
         sys.path.insert(0, str(d))
     _mods = {}
-    for name in ("cyutils", "pca", "normalize", "cysparse", "hvg", "ref_probe"):
+    for name in ("cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn",
+                 "ref_probe"):
         try:
             _mods[name] = importlib.import_module(f"brisc.{name}")
         except ImportError:
-            if name not in ("cysparse", "hvg"):
+            if name not in ("cysparse", "hvg", "kmeans", "knn"):
                 raise
     return _mods
 
@@ -142,3 +143,99 @@ def run_irlba(indptr, indices, data_f32, n: int, g: int, k: int = 50,
             match_parallel=bool(match_parallel), is_csr=True,
             num_threads=num_threads, chunk_size=chunk_size, PCs=PCs)
     return PCs, bool(conv)
+
+
+def run_kmeans_for_knn(PCs, num_neighbors: int = 20, num_clusters=None,
+                       num_clusters_searched=None, num_kmeans_iterations: int = 2,
+                       kmeans_tolerance: float = 1e-2, kmeans_barbar: bool = False,
+                       num_init_iterations: int = 5, oversampling_factor: float = 1,
+                       chunk_size_kmeans=None, chunk_size_search=None, seed: int = 0,
+                       num_threads: int | None = None) -> dict:
+    """The k-means half of the reference's neighbors() on a float32 PCs array
+    (every cell passing QC): its compiled kmeans (brisc/kmeans.pyx:889), then
+    the argument preparation of brisc/single_cell.py:12451-12611 -- default
+    cluster counts and chunk sizes, empty-cluster removal, the minimum number
+    of clusters searched, centroids ordered by PC 1, cells sorted by cluster.
+    Returns every input knn_self (brisc/knn.pyx:13) takes, as a dict."""
+    M = load()
+    kmeans = M["kmeans"].kmeans
+    X = np.ascontiguousarray(PCs, dtype=np.float32)
+    num_threads = num_threads or os.cpu_count() or 1
+    n, d = X.shape
+    if num_clusters is None:
+        num_clusters = max(1, int(np.ceil(min(4 * np.sqrt(n), n / 100))))
+    if num_clusters_searched is None:
+        num_clusters_searched = min(64, num_clusters)
+    if chunk_size_kmeans is None:
+        chunk_size_kmeans = min(4096, n)
+    if chunk_size_search is None:
+        chunk_size_search = min(256, n)
+    labels = np.zeros(n, dtype=np.uint32)
+    min_distances = np.zeros(n, dtype=np.float32)
+    cell_norms = np.zeros(n, dtype=np.float32)
+    centroids = np.empty((num_clusters, d), dtype=np.float32)
+    centroids_new = np.empty((num_clusters, d), dtype=np.float32)
+    counts = np.empty(num_clusters, dtype=np.uint32)
+    with _blas1():
+        it = kmeans(X=X, cluster_labels=labels, centroids=centroids,
+                    centroids_new=centroids_new, num_cells_per_cluster=counts,
+                    min_distances=min_distances, cell_norms=cell_norms,
+                    kmeans_barbar=kmeans_barbar,
+                    num_init_iterations=num_init_iterations,
+                    num_kmeans_iterations=num_kmeans_iterations,
+                    tolerance=kmeans_tolerance,
+                    oversampling_factor=oversampling_factor, seed=seed,
+                    chunk_size=chunk_size_kmeans, is_mac=False,
+                    num_threads=num_threads)
+    if it & 1:
+        centroids = centroids_new
+    non_empty = counts > 0
+    if not non_empty.all():
+        centroids = centroids[non_empty]
+        counts = counts[non_empty]
+        num_clusters = len(centroids)
+        remap = np.zeros(len(non_empty), dtype=np.uint32)
+        remap[non_empty] = np.arange(num_clusters, dtype=np.uint32)
+        labels = remap[labels]
+    cumsum = np.sort(counts).cumsum(dtype=np.uint64)
+    min_searched = int(np.searchsorted(cumsum, num_neighbors + 1)) + 1
+    num_clusters_searched = min(max(num_clusters_searched, min_searched), num_clusters)
+    order = np.argsort(centroids[:, 0]).astype(np.uint32)
+    centroids = np.ascontiguousarray(centroids[order])
+    counts = np.ascontiguousarray(counts[order])
+    inv = np.empty_like(order)
+    inv[order] = np.arange(len(order), dtype=np.uint32)
+    labels = inv[labels]
+    sorted_order = np.argsort(labels).astype(np.uint32)
+    return dict(X=np.ascontiguousarray(X[sorted_order]), sorted_order=sorted_order,
+                centroids=centroids, num_cells_per_cluster=counts,
+                cell_norms=np.ascontiguousarray(cell_norms[sorted_order]),
+                num_neighbors=int(num_neighbors),
+                num_clusters_searched=int(num_clusters_searched),
+                chunk_size_kmeans=int(chunk_size_kmeans),
+                chunk_size_search=int(chunk_size_search))
+
+
+def run_knn_self(prep: dict, num_threads: int | None = None):
+    """The reference's knn_self (brisc/knn.pyx:13) on run_kmeans_for_knn's
+    outputs. Returns (neighbors, distances) in cluster-sorted row order, as
+    knn_self leaves them (squared Euclidean distances, self excluded,
+    neighbour indices already mapped to the original cell order)."""
+    M = load()
+    n = prep["X"].shape[0]
+    k, cs = prep["num_neighbors"], prep["num_clusters_searched"]
+    neighbors = np.zeros((n, k), dtype=np.uint32)
+    distances = np.zeros((n, k), dtype=np.float32)
+    cdist = np.zeros((n, cs), dtype=np.float32)
+    near = np.zeros((n, cs), dtype=np.uint32)
+    with _blas1():
+        M["knn"].knn_self(
+            X=prep["X"], sorted_order=prep["sorted_order"],
+            centroids=prep["centroids"],
+            num_cells_per_cluster=prep["num_cells_per_cluster"],
+            neighbors=neighbors, distances=distances, cell_norms=prep["cell_norms"],
+            centroid_distances=cdist, nearest_clusters=near, num_neighbors=k,
+            num_clusters_searched=cs, chunk_size_kmeans=prep["chunk_size_kmeans"],
+            chunk_size_search=prep["chunk_size_search"], is_mac=False,
+            num_threads=num_threads or os.cpu_count() or 1)
+    return neighbors, distances, near, cdist
