@@ -129,6 +129,8 @@ SIGNATURES = {
     "bgpu_csr_tocsc": (_i, [_u64, _u32, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "bgpu_gene_mean_var": (_i, [C.POINTER(HvgInput), _u64, _vp, _vp, _vp, _vp]),
     "bgpu_clipped_sum": (_i, [C.POINTER(HvgInput), _u64, _vp, _vp, _vp, _vp]),
+    "bgpu_knn_self": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _u32,
+                           _u32, _u32, _u32, _vp]),
 }
 
 _lock = threading.Lock()

@@ -338,6 +338,32 @@ BGPU_API int bgpu_clipped_sum(const bgpu_hvg_input* in, uint64_t num_cells,
                               const float* clip_val, float* batch_counts_sum,
                               float* squared_batch_counts_sum, void* stream);
 
+/* ---- k-nearest neighbours on the principal components ----------------- */
+/* knn_self (brisc/knn.pyx:13-515, called by SingleCell.neighbors at
+ * brisc/single_cell.py:12613-12626): for every cell of X (num_cells x
+ * num_dimensions, row-major float32, rows grouped by k-means cluster), the
+ * num_neighbors nearest other cells among the cells of its
+ * num_clusters_searched nearest clusters. Same arguments as the reference,
+ * minus its chunk sizes, is_mac and num_threads (CPU scheduling knobs with no
+ * effect on the result): sorted_order maps a row of X to the original cell
+ * id; centroids (num_clusters x num_dimensions) and num_cells_per_cluster
+ * (uint32, summing to num_cells) describe the clusters in row order;
+ * cell_norms holds each row's squared norm. Outputs, row-major per row of X:
+ * neighbors (num_cells x num_neighbors, original ids) and distances (squared
+ * Euclidean |x|^2 + |c|^2 - 2 x.c) in ascending distance, and
+ * nearest_clusters / centroid_distances (num_cells x num_clusters_searched)
+ * in ascending partial distance |c|^2 - 2 x.c. All pointers are device
+ * pointers. Limits: num_dimensions <= 128, num_neighbors <= 128,
+ * num_clusters_searched <= 256, num_clusters <= 32768. Synchronous. */
+BGPU_API int bgpu_knn_self(const float* X, const uint32_t* sorted_order,
+                           const float* centroids,
+                           const uint32_t* num_cells_per_cluster, uint32_t* neighbors,
+                           float* distances, const float* cell_norms,
+                           float* centroid_distances, uint32_t* nearest_clusters,
+                           uint64_t num_cells, uint32_t num_dimensions,
+                           uint32_t num_clusters, uint32_t num_neighbors,
+                           uint32_t num_clusters_searched, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,6 +18,12 @@ reference's outputs, so the tests never regenerate data:
                  FP64 from the reference's PCs), the convergence flag, the
                  reference's own accuracy against the FP64 oracle, and a
                  fingerprint of the seeded input.
+* knn.npz        knn_self (brisc/knn.pyx:13) after the reference's kmeans
+                 (brisc/kmeans.pyx:889) and neighbors()'s argument
+                 preparation (brisc/single_cell.py:12451-12611), on seeded
+                 Gaussian-mixture "PCs" (regenerated from the seed, with a
+                 fingerprint): the k-means outputs knn_self takes and its
+                 neighbours, distances and nearest clusters.
 * hvg.npz        gene_mean_and_variance_csr/_csc and clipped_sum_csr/_csc
                  (brisc/hvg.pyx) on an NB count matrix with a few large
                  counts, over all cells and over a cell subset, uint32 and
@@ -26,6 +32,7 @@ reference's outputs, so the tests never regenerate data:
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py hvg      # hvg.npz only
     python tests/golden/make_golden.py parity   # parity50k.npz only
+    python tests/golden/make_golden.py knn      # knn.npz only
 """
 from __future__ import annotations
 
@@ -115,6 +122,45 @@ def make_parity() -> None:
     np.savez_compressed(OUT / "parity50k.npz", **out)
 
 
+KNN_CASES = {  # name: (cells, dims, components, seed, num_neighbors, clusters searched)
+    "knn_a": (8000, 20, 24, 3, 12, 12),
+    "knn_b": (3000, 8, 10, 4, 5, None),
+}
+
+
+def knn_pcs(n: int, d: int, comps: int, seed: int) -> np.ndarray:
+    """Seeded stand-in for principal components: a Gaussian mixture with
+    per-dimension scales falling like a PCA spectrum. Regenerated by the
+    tests from the seed (numpy's Generator streams are stable)."""
+    rng = np.random.default_rng(seed)
+    scale = 10.0 / np.sqrt(1.0 + np.arange(d))
+    centres = rng.standard_normal((comps, d)) * scale
+    lab = rng.integers(0, comps, n)
+    X = centres[lab] + 0.35 * rng.standard_normal((n, d)) * scale
+    return np.ascontiguousarray(X.astype(np.float32))
+
+
+def make_knn() -> None:
+    import hashlib
+    out = {}
+    for name, (n, d, comps, seed, k, cs) in KNN_CASES.items():
+        X = knn_pcs(n, d, comps, seed)
+        prep = ref.run_kmeans_for_knn(X, num_neighbors=k, num_clusters_searched=cs,
+                                      seed=0, num_threads=1)
+        nbr, dist, near, cdist = ref.run_knn_self(prep, num_threads=1)
+        out[f"{name}_shape"] = np.array([n, d, comps, seed, k, prep["num_clusters_searched"]])
+        out[f"{name}_fingerprint"] = np.array(hashlib.sha256(X.tobytes()).hexdigest())
+        for key in ("sorted_order", "centroids", "num_cells_per_cluster", "cell_norms"):
+            out[f"{name}_{key}"] = prep[key]
+        out[f"{name}_neighbors"] = nbr
+        out[f"{name}_distances"] = dist
+        out[f"{name}_nearest_clusters"] = near
+        out[f"{name}_centroid_distances"] = cdist
+        print(name, "clusters", len(prep["centroids"]), "searched",
+              prep["num_clusters_searched"])
+    np.savez_compressed(OUT / "knn.npz", **out)
+
+
 def main() -> int:
     M = ref.load()
     if M is None:
@@ -123,8 +169,13 @@ def main() -> int:
     if sys.argv[1:] == ["parity"]:
         make_parity()
         return 0
+    if sys.argv[1:] == ["knn"]:
+        make_knn()
+        return 0
     if "hvg" in M:
         make_hvg(M)
+    if "knn" in M and not sys.argv[1:]:
+        make_knn()
     if sys.argv[1:] == ["hvg"]:
         return 0
     probe = M["ref_probe"]

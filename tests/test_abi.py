@@ -115,3 +115,27 @@ def test_hvg_arguments_rejected_without_gpu(built_lib):
     assert run(is_csr=0, num_genes=5) == _lib.ERR_INVALID
     assert b"fewer genes" in L.bgpu_last_error()
     assert L.bgpu_gene_mean_var(None, 1, None, None, None, None) == _lib.ERR_INVALID
+
+
+def test_knn_self_argument_checks_before_any_device_work():
+    """The knn_self drop-in rejects wrong dtypes, shapes and chunk sizes with
+    the reference caller's errors before touching the GPU."""
+    import pytest as _pt
+    from brisc_gb300 import knn
+    n, d, k, cs, nc = 10, 3, 2, 2, 2
+    good = dict(X=np.zeros((n, d), np.float32), sorted_order=np.arange(n, dtype=np.uint32),
+                centroids=np.zeros((nc, d), np.float32),
+                num_cells_per_cluster=np.array([5, 5], np.uint32),
+                neighbors=np.zeros((n, k), np.uint32), distances=np.zeros((n, k), np.float32),
+                cell_norms=np.zeros(n, np.float32),
+                centroid_distances=np.zeros((n, cs), np.float32),
+                nearest_clusters=np.zeros((n, cs), np.uint32), num_neighbors=k,
+                num_clusters_searched=cs)
+    bad = dict(good, X=np.zeros((n, d), np.float64))
+    with _pt.raises(TypeError):
+        knn.knn_self(**bad)
+    bad = dict(good, neighbors=np.zeros((n, k + 1), np.uint32))
+    with _pt.raises(ValueError):
+        knn.knn_self(**bad)
+    with _pt.raises(ValueError, match="chunk_size_search"):
+        knn.knn_self(**good, chunk_size_search=0)

@@ -186,3 +186,18 @@ def test_oracle_adaptive_mode_second_passes_where_needed(golden):
     assert 0 < o["second_passes"] < o["steps"] - 1
     S, U, Vt = dense.top_svd(X.astype(np.float64), 8)
     assert dense.rel_sv_error(o["PCs"], S).max() < 1e-4
+
+
+@pytest.mark.parametrize("name", ["knn_a", "knn_b"])
+def test_knn_oracle_matches_reference(golden, name):
+    """oracle/knn.py (the NumPy restatement of brisc/knn.pyx:13) against the
+    compiled reference's knn_self on the fixture's k-means outputs: the same
+    nearest clusters and neighbour sets up to FP32 near-ties, distances
+    within FP32 rounding of the squared norms."""
+    from knn_cases import case, check_against
+    from oracle import knn as oknn
+    c = case(golden("knn"), name)
+    nbr, dist, near, cdist = oknn.knn_self(
+        c["X"], c["sorted_order"], c["centroids"], c["num_cells_per_cluster"],
+        c["cell_norms"], c["num_neighbors"], c["num_clusters_searched"])
+    check_against(c, nbr, dist, near, cdist)
