@@ -56,6 +56,8 @@ WORKLOADS = {
     "serve": (0, 0, 0.0, 0, 0),
     # HVG gene statistics (brisc/hvg.pyx) over the same 1M x 2000 counts
     "hvg_1m": (1_000_000, 2000, 0.05, 0, 0),
+    # knn_self (brisc/knn.pyx) on 1M cells x 50 PCs, 20 neighbours
+    "knn_1m": (1_000_000, 50, 0.0, 20, 0),
 }
 # Generator arguments beyond the density: the large solve has 13 cell-type
 # clusters with lognormal(0, 0.8) per-gene mean offsets; their mean factor
@@ -807,12 +809,149 @@ def run_hvg(args):
     return 0
 
 
+def neighbour_agreement(X, so, norms, a, b) -> dict:
+    """How two knn_self results compare: rows whose neighbour sets are
+    identical, and on the others the worst distance of a differing neighbour
+    inside the other list's k-th distance, in units of FP32 rounding of the
+    squared norms (<= 1: a near-tie either side may break)."""
+    from oracle import knn as oknn
+    same = np.all(np.sort(a, 1) == np.sort(b, 1), axis=1)
+    rows = np.flatnonzero(~same)
+    _, worst = oknn.compare(X, so, norms, a, b, rows=rows[:20000])
+    return {"rows_identical": float(same.mean()), "rows_checked": int(min(len(rows), 20000)),
+            "worst_tie_excess": float(worst)}
+
+
+def run_knn(args):
+    """knn_self (brisc/knn.pyx:13) over 1M cells x 50 PCs (seeded Gaussian
+    mixture with a PCA-like spectrum), 20 neighbours, the reference's default
+    cluster counts: its own k-means (brisc/kmeans.pyx:889, compiled from its
+    sources, run once on the host, untimed) makes the inputs. A step is one
+    knn_self on device-resident inputs; e2e is the same call from host arrays
+    through the drop-in (copies included). The reference's knn_self on every
+    host core is the CPU baseline and the parity check."""
+    import ctypes as C
+
+    import torch
+
+    from brisc_gb300 import _lib as L
+    from brisc_gb300 import knn
+    from oracle import ref
+    from synth import pca_like
+    torch.cuda.init()
+    dev = torch.device("cuda", 0)
+    n, d, _, k, _ = WORKLOADS[args.workload]
+    if args.cells:
+        n = args.cells
+    X = pca_like(n, d, 40, seed=0)
+    if ref.load() is None or "kmeans" not in ref.load():
+        print(json.dumps({"workload": args.workload, "unavailable":
+                          "the reference's kmeans could not be built on this host"}))
+        return 0
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    prep = ref.run_kmeans_for_knn(X, num_neighbors=k, seed=0, num_threads=cores)
+    t_kmeans = time.perf_counter() - t0
+    cs, nc = prep["num_clusters_searched"], len(prep["centroids"])
+
+    def T(a):
+        return torch.from_numpy(np.ascontiguousarray(
+            a.view(np.int32) if a.dtype == np.uint32 else a)).to(dev)
+    dX, dso, dC, dcnt, dnrm = (T(prep[key]) for key in
+                               ("X", "sorted_order", "centroids", "num_cells_per_cluster",
+                                "cell_norms"))
+    dnb = torch.zeros((n, k), dtype=torch.int32, device=dev)
+    ddi = torch.zeros((n, k), dtype=torch.float32, device=dev)
+    dcd = torch.zeros((n, cs), dtype=torch.float32, device=dev)
+    dnc = torch.zeros((n, cs), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp_ = C.c_void_p(stream.cuda_stream)
+
+    def step():
+        L.call("bgpu_knn_self", dX.data_ptr(), dso.data_ptr(), dC.data_ptr(),
+               dcnt.data_ptr(), dnb.data_ptr(), ddi.data_ptr(), dnrm.data_ptr(),
+               dcd.data_ptr(), dnc.data_ptr(), n, d, nc, k, cs, sp_)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / args.steps
+    gpu_nbr = dnb.cpu().numpy().view(np.uint32)
+
+    # e2e: host arrays through the drop-in
+    hn = np.zeros((n, k), np.uint32)
+    hd = np.zeros((n, k), np.float32)
+    hcd = np.zeros((n, cs), np.float32)
+    hnc = np.zeros((n, cs), np.uint32)
+    e2e_steps = args.e2e_steps or min(3, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        knn.knn_self(X=prep["X"], sorted_order=prep["sorted_order"],
+                     centroids=prep["centroids"],
+                     num_cells_per_cluster=prep["num_cells_per_cluster"],
+                     neighbors=hn, distances=hd, cell_norms=prep["cell_norms"],
+                     centroid_distances=hcd, nearest_clusters=hnc, num_neighbors=k,
+                     num_clusters_searched=cs, num_threads=cores)
+    e2e = (time.perf_counter() - t0) / e2e_steps
+    same_paths = bool(np.array_equal(hn, gpu_nbr))
+
+    # candidate FLOPs: n C d for the nearest clusters, sum of searched
+    # cluster sizes x d for the neighbour search (2 flop per multiply-add)
+    near = hnc.astype(np.int64)
+    cand = prep["num_cells_per_cluster"].astype(np.int64)[near].sum()
+    flops = 2.0 * d * (n * nc + cand)
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, nominal SIMT FP32
+    cpu, parity = None, None
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        rnb, rdi, rnc, _ = ref.run_knn_self(prep, num_threads=cores)
+        t_ref = time.perf_counter() - t0
+        cpu = {"value": t_ref, "unit": "s/search", "cores": cores, "kind": "reference",
+               "sample": "the reference's knn_self on the full 1M-cell input, every "
+                         "host core (its k-means outside the timing, as here)"}
+        parity = neighbour_agreement(prep["X"], prep["sorted_order"], prep["cell_norms"],
+                                     hn, rnb)
+        parity["nearest_clusters_rows_identical"] = float(
+            np.all(np.sort(hnc, 1) == np.sort(rnc, 1), axis=1).mean())
+    out = {"metric": "knn_self: s per search (1M cells x 50 PCs, 20 neighbours)",
+           "value": sec, "unit": "s/search", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "higher_is_better": False, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": f"knn_1m: {n:,} cells x {d} PCs (Gaussian mixture, "
+                                  f"PCA-like spectrum), {k} neighbours, {nc} k-means "
+                                  f"clusters, {cs} searched",
+                      "l2": "inputs (200 MB PCs) larger than L2 (no flush)",
+                      "kmeans_seconds_host": t_kmeans},
+           "e2e": {"value": e2e, "unit": "s/search",
+                   "h2d_bytes_per_step": int(X.nbytes + n * 8 + nc * (d + 1) * 4),
+                   "d2h_bytes_per_step": int(n * (k + cs) * 8)},
+           "roofline": {"bound": "fp32-simt", "achieved": flops / sec / 1e12,
+                        "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": flops / sec / 1e12 / fp32_peak,
+                        "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz)",
+                        "traffic": None, "flops_per_step": flops},
+           "cpu_baseline": cpu, "agreement_with_reference": parity,
+           "host_and_device_paths_identical": same_paths,
+           "clocks": clk.summary(), "gpu_launches": 4 * args.steps}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "hvg_1m":
         return run_hvg(args)
+    if args.workload == "knn_1m":
+        return run_knn(args)
     if args.workload == "batched_3m":
         return run_batched(args)
     if args.workload == "serve":

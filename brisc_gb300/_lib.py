@@ -18,6 +18,9 @@ INDEX_I32, INDEX_I64 = 0, 1
 VALUE_U16, VALUE_U32, VALUE_I32, VALUE_F32 = 0, 1, 2, 3
 VALUE_I64, VALUE_U64, VALUE_F64 = 4, 5, 6  # the HVG statistics only
 NORM_NONE, NORM_LOGCP10K, NORM_LOG1PPF, NORM_PFLOG1PPF = -1, 0, 1, 2
+# forced product kernels (bgpu_matrix_desc.kernels)
+KERNELS = {"panels": 1, "natural": 2, "words32": 4, "xv_rows": 8, "xv_seg": 16,
+           "vector": 32}
 
 
 class MatrixDesc(C.Structure):
@@ -35,6 +38,7 @@ class MatrixDesc(C.Structure):
         ("inv_size_factors", C.c_void_p),
         ("post_factors", C.c_void_p),
         ("panel_rows", C.c_uint32),
+        ("kernels", C.c_uint32),
     ]
 
 

@@ -643,13 +643,10 @@ static void choose_shapes(Matrix& m) {
   // X.v kernel: the segmented stream keeps every lane busy on short rows;
   // 8 lanes per row amortise their per-row work better on long ones.
   m.spmv_seg = m.csr_heads && avg < 64.0;
-  // BGPU_SPMV_IMPL = vector | rows | seg overrides the choice (A/B study)
-  if (const char* e = std::getenv("BGPU_SPMV_IMPL")) {
-    const std::string k(e);
-    m.impl = k == "vector" ? 1 : 0;
-    if (k == "rows") m.spmv_seg = false;
-    if (k == "seg") m.spmv_seg = m.csr_heads;
-  }
+  // forced choices (bgpu_matrix_desc.kernels)
+  if (m.kernels & BGPU_KERNELS_VECTOR) m.impl = 1;
+  if (m.kernels & BGPU_KERNELS_XV_ROWS) m.spmv_seg = false;
+  if (m.kernels & BGPU_KERNELS_XV_SEG) m.spmv_seg = m.csr_heads;
 }
 
 extern "C" int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* d,

@@ -334,6 +334,8 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
                BGPU_ERR_INVALID, "unknown norm_method");
   BGPU_REQUIRE(d->indptr && (d->nnz == 0 || (d->indices && d->values)),
                BGPU_ERR_INVALID, "indptr/indices/values must not be NULL");
+  BGPU_REQUIRE((d->kernels & ~63u) == 0, BGPU_ERR_INVALID, "unknown BGPU_KERNELS_* bits");
+  m->kernels = d->kernels;
   if (d->norm_method == BGPU_NORM_NONE) {
     BGPU_REQUIRE(d->value_type == BGPU_VALUE_F32, BGPU_ERR_INVALID,
                  "pre-normalised input (BGPU_NORM_NONE) must be float32");
@@ -490,7 +492,7 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
 
   // Sliced-ELL layout for both products where it applies (counts, <= 4096
   // genes); the packed CSR words were only its source then.
-  if (m->mode == kCounts) {
+  if (m->mode == kCounts && !(m->kernels & BGPU_KERNELS_PANELS)) {
     bool built = false;
     BGPU_TRY(build_sell(m, s, &built));
     if (built) {

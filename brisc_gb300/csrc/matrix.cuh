@@ -122,6 +122,7 @@ struct Matrix {
   bool spmv_seg = false;   // X.v by the segmented stream (short rows) rather
                            // than 8 lanes per row
   int impl = 0;            // 0 = table-driven kernels, 1 = register-vector kernels
+  uint32_t kernels = 0;    // bgpu_matrix_desc.kernels (BGPU_KERNELS_*)
 
   // Sliced-ELL layout (sell.cu), counts mode with g <= 4096: when `sell` is
   // set both products run on it and the panel layout above is not built.

@@ -665,10 +665,10 @@ __global__ void k_count_tables(const float* __restrict__ isf, uint64_t n,
 
 // Row order for X.v (matrix creation): rows by descending count of 32-entry
 // windows (the 8-lane groups' passes), stable, by a counting sort on the host.
-// BGPU_ROW_ORDER=0 keeps the natural order (A/B study).
+// BGPU_KERNELS_NATURAL keeps the natural order.
 int build_row_order(Matrix* m, cudaStream_t s, uint64_t* bytes_acc) {
-  const char* e = std::getenv("BGPU_ROW_ORDER");
-  if ((e && e[0] == '0') || m->n < 2 || m->n >= (uint64_t)INT32_MAX) return BGPU_OK;
+  if ((m->kernels & BGPU_KERNELS_NATURAL) || m->n < 2 || m->n >= (uint64_t)INT32_MAX)
+    return BGPU_OK;
   std::vector<int64_t> rp(m->n + 1);
   BGPU_CUDA(cudaMemcpyAsync(rp.data(), m->rowptr, (m->n + 1) * 8, cudaMemcpyDeviceToHost, s));
   BGPU_CUDA(cudaStreamSynchronize(s));
@@ -721,9 +721,8 @@ int build_stream_tiles(Matrix* m, const std::vector<int64_t>& panel_rowptr,
   }
   BGPU_TRY(build_row_order(m, s, bytes_acc));
   m->stream_ok = true;
-  // BGPU_COMPACT=0 keeps X^T.u on the 32-bit panel words (A/B study)
-  const char* ec = std::getenv("BGPU_COMPACT");
-  if (!(ec && ec[0] == '0')) BGPU_TRY(build_compact16(m, s, bytes_acc));
+  // BGPU_KERNELS_WORDS32 keeps X^T.u on the 32-bit panel words
+  if (!(m->kernels & BGPU_KERNELS_WORDS32)) BGPU_TRY(build_compact16(m, s, bytes_acc));
   return BGPU_OK;
 }
 

@@ -84,8 +84,16 @@ def irlba(data_matvec, indices_matvec, indptr_matvec, data_rmatvec,
     rmatvec, ``PCs`` a preallocated C-contiguous float32 (num_cells, k) array
     filled in place. Returns whether IRLBA converged. The CSC arrays are
     accepted for compatibility; the GPU builds its own transposed copy.
+    ``chunk_size`` sets the reference's reduction blocks (pca.pyx:1006-1010),
+    which change only the rounding of its sums; the GPU sums over fixed
+    1024-row blocks whatever it is, and warns when it is not 1024.
     """
     num_cells, num_genes, k = int(num_cells), int(num_genes), int(k)
+    if int(chunk_size) != 1024:
+        import warnings
+        warnings.warn(f"chunk_size={int(chunk_size)}: the GPU solve reduces over fixed "
+                      "1024-row blocks (the value only changes the reference's "
+                      "rounding)", RuntimeWarning, stacklevel=2)
     _check_vec(data_matvec, "data_matvec", np.float32)
     idx_t = indices_matvec.dtype
     if idx_t not in _INDEX_TYPES:
@@ -140,10 +148,12 @@ class DeviceMatrix:
     def __init__(self, indptr, indices, values, num_cells: int,
                  num_genes: int, *, norm: str | None = None,
                  inv_size_factors=None, post_factors=None,
-                 panel_rows: int = 0, stream=None, rows=None):
+                 panel_rows: int = 0, stream=None, rows=None, kernels=()):
         """``rows`` (int64 cell indices, NumPy for host inputs or a CUDA
         tensor for device inputs) selects the row subset X[rows, :]: the
-        matrix is then that subset, with its own gene centring and scaling."""
+        matrix is then that subset, with its own gene centring and scaling.
+        ``kernels`` (names of _lib.KERNELS) forces product-kernel choices,
+        for comparing layouts; the default picks them automatically."""
         on_dev = not isinstance(indptr, np.ndarray)
         idx_dt = _np_dtype(indices)
         if idx_dt != _np_dtype(indptr) or idx_dt not in _INDEX_TYPES:
@@ -162,6 +172,9 @@ class DeviceMatrix:
         d.inv_size_factors = _ptr(inv_size_factors)
         d.post_factors = _ptr(post_factors)
         d.panel_rows = int(panel_rows)
+        d.kernels = 0
+        for name in kernels:
+            d.kernels |= L.KERNELS[name]
         self._keep = (indptr, indices, values, inv_size_factors, post_factors)
         h = C.c_void_p()
         if rows is None:

@@ -102,7 +102,22 @@ typedef struct bgpu_matrix_desc {
   const float* post_factors;
   /* Rows per transposed panel (power of two in [1024, 65536]); 0 = automatic. */
   uint32_t panel_rows;
+  /* Product kernels: 0 = automatic (the sliced-ELL layout for counts with at
+   * most 4096 genes, else the panel layout with rules on the mean entries per
+   * row). Nonzero: an OR of BGPU_KERNELS_* forcing a choice, for comparing
+   * layouts; every choice computes the same products to FP32 rounding, in
+   * its own fixed order. No counterpart in the reference. */
+  uint32_t kernels;
 } bgpu_matrix_desc;
+
+enum {
+  BGPU_KERNELS_PANELS = 1,   /* panel layout even where sliced-ELL applies    */
+  BGPU_KERNELS_NATURAL = 2,  /* panel X.v rows in natural, not length, order  */
+  BGPU_KERNELS_WORDS32 = 4,  /* panel X^T.u over the 32-bit words             */
+  BGPU_KERNELS_XV_ROWS = 8,  /* panel X.v: 8 lanes per row                    */
+  BGPU_KERNELS_XV_SEG = 16,  /* panel X.v: segmented stream (needs row heads) */
+  BGPU_KERNELS_VECTOR = 32   /* register-vector kernels instead of tables     */
+};
 
 BGPU_API int bgpu_matrix_create(bgpu_matrix** out, const bgpu_matrix_desc* desc,
                        void* stream);

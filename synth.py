@@ -169,3 +169,16 @@ def cached_nb_counts(num_cells: int, num_genes: int = 2000, seed: int = 0,
     except OSError:
         pass
     return M
+
+
+def pca_like(num_cells: int, num_dims: int, components: int, seed: int) -> np.ndarray:
+    """Seeded stand-in for principal components (float32, C order): a Gaussian
+    mixture of ``components`` centres whose per-dimension scale falls like a
+    PCA spectrum (10 / sqrt(1 + dim)), each cell its centre plus 0.35-scaled
+    noise. Used where a kNN search needs PCs of a given shape."""
+    rng = np.random.default_rng(seed)
+    scale = 10.0 / np.sqrt(1.0 + np.arange(num_dims))
+    centres = rng.standard_normal((components, num_dims)) * scale
+    lab = rng.integers(0, components, num_cells)
+    X = centres[lab] + 0.35 * rng.standard_normal((num_cells, num_dims)) * scale
+    return np.ascontiguousarray(X.astype(np.float32))

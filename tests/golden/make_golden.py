@@ -129,15 +129,10 @@ KNN_CASES = {  # name: (cells, dims, components, seed, num_neighbors, clusters s
 
 
 def knn_pcs(n: int, d: int, comps: int, seed: int) -> np.ndarray:
-    """Seeded stand-in for principal components: a Gaussian mixture with
-    per-dimension scales falling like a PCA spectrum. Regenerated by the
-    tests from the seed (numpy's Generator streams are stable)."""
-    rng = np.random.default_rng(seed)
-    scale = 10.0 / np.sqrt(1.0 + np.arange(d))
-    centres = rng.standard_normal((comps, d)) * scale
-    lab = rng.integers(0, comps, n)
-    X = centres[lab] + 0.35 * rng.standard_normal((n, d)) * scale
-    return np.ascontiguousarray(X.astype(np.float32))
+    """Seeded stand-in for principal components (synth.pca_like), regenerated
+    by the tests from the seed (numpy's Generator streams are stable)."""
+    from synth import pca_like
+    return pca_like(n, d, comps, seed)
 
 
 def make_knn() -> None:

@@ -9,13 +9,9 @@ import numpy as np
 
 def knn_pcs(n: int, d: int, comps: int, seed: int) -> np.ndarray:
     """The seeded Gaussian-mixture stand-in for principal components that
-    tests/golden/make_golden.py fed the reference."""
-    rng = np.random.default_rng(seed)
-    scale = 10.0 / np.sqrt(1.0 + np.arange(d))
-    centres = rng.standard_normal((comps, d)) * scale
-    lab = rng.integers(0, comps, n)
-    X = centres[lab] + 0.35 * rng.standard_normal((n, d)) * scale
-    return np.ascontiguousarray(X.astype(np.float32))
+    tests/golden/make_golden.py fed the reference (synth.pca_like)."""
+    from synth import pca_like
+    return pca_like(n, d, comps, seed)
 
 
 def case(z, name: str) -> dict:

@@ -110,10 +110,14 @@ def _normalized(X, isf, post=None):
 @pytest.mark.parametrize("mode", ["counts", "counts_post", "float"])
 @pytest.mark.parametrize("itype", [np.int32, np.int64])
 @pytest.mark.parametrize("panel_rows", [0, 2048])
-@pytest.mark.parametrize("impl", ["rows", "seg", "vector"])
-def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows, impl, monkeypatch):
+@pytest.mark.parametrize("impl", ["auto", "rows", "seg", "vector", "words32"])
+def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows, impl):
+    """Both sparse products and the gene std on every layout: automatic
+    (sliced-ELL for counts), and the panel layout with each X.v kernel and
+    with X^T.u over the 32-bit words."""
     import torch
-    monkeypatch.setenv("BGPU_SPMV_IMPL", impl)
+    kernels = {"auto": (), "rows": ("panels", "xv_rows"), "seg": ("panels", "xv_seg"),
+               "vector": ("panels", "vector"), "words32": ("panels", "words32")}[impl]
     X, isf = _mat()
     n, g = X.shape
     post = None
@@ -123,14 +127,14 @@ def test_matvec_rmatvec_stddev(cuda, mode, itype, panel_rows, impl, monkeypatch)
     ip, ix = X.indptr.astype(itype), X.indices.astype(itype)
     if mode == "counts":
         M = DeviceMatrix(ip, ix, X.data.astype(np.uint16), n, g, norm="logCP10k",
-                         inv_size_factors=isf, panel_rows=panel_rows)
+                         inv_size_factors=isf, panel_rows=panel_rows, kernels=kernels)
     elif mode == "counts_post":
         M = DeviceMatrix(ip, ix, X.data.astype(np.uint16), n, g, norm="PFlog1pPF",
                          inv_size_factors=isf, post_factors=post,
-                         panel_rows=panel_rows)
+                         panel_rows=panel_rows, kernels=kernels)
     else:
         M = DeviceMatrix(ip, ix, Xn.data.astype(np.float32), n, g,
-                         panel_rows=panel_rows)
+                         panel_rows=panel_rows, kernels=kernels)
     rng = np.random.default_rng(0)
     v = rng.standard_normal(g).astype(np.float32)
     u = rng.standard_normal(n).astype(np.float32)
@@ -287,18 +291,17 @@ def test_rotate_basis_ritz_rotation_unbiased(cuda, rows, K, ncols):
     np.testing.assert_array_equal(out[2][0], -A[3, :rows].astype(np.float64))
 
 
-def test_row_order_does_not_change_products(cuda, monkeypatch):
+def test_row_order_does_not_change_products(cuda):
     """X.v with the length-ordered row schedule is bit-identical to the natural
     order: the schedule only changes which 8-lane group sums a row."""
     import torch
     X, isf = _mat(n=9000, g=600, density=0.08)
     n, g = X.shape
     out = []
-    for order in ("1", "0"):
-        monkeypatch.setenv("BGPU_ROW_ORDER", order)
+    for kernels in (("panels", "xv_rows"), ("panels", "xv_rows", "natural")):
         M = DeviceMatrix(X.indptr.astype(np.int32), X.indices.astype(np.int32),
                          X.data.astype(np.uint16), n, g, norm="logCP10k",
-                         inv_size_factors=isf)
+                         inv_size_factors=isf, kernels=kernels)
         v = T(np.random.default_rng(3).standard_normal(g).astype(np.float32), cuda)
         sd = torch.ones(g, dtype=torch.float32, device=cuda)
         y = torch.empty(n, dtype=torch.float32, device=cuda)
