@@ -489,16 +489,21 @@ int launch_jacobi_svd(const float* Bf, const double* Bd, uint32_t m, float* Ub,
   const bool use_smem = smem <= 220 * 1024;
   BGPU_REQUIRE(use_smem || gwork, BGPU_ERR_INVALID,
                "small SVD of this size needs a global workspace");
+  // one 8-lane group per pair of a round, in whole warps: a small matrix
+  // gets a small block and cheap barriers (each pair's arithmetic, and so
+  // the result, does not depend on the block size)
+  const unsigned threads = (unsigned)std::min<uint64_t>(
+      1024, std::max<uint64_t>(64, round_up(8ull * ((m + 1) / 2), 32)));
   if (fp64) {
     if (use_smem && smem > 48 * 1024)
       BGPU_CUDA(allow_max_smem(k_jacobi<double>));
-    k_jacobi<double><<<1, 1024, use_smem ? smem : 0, s>>>(
+    k_jacobi<double><<<1, threads, use_smem ? smem : 0, s>>>(
         Bd, m, Ub, Sb, Vbt, ub_last, sb64, ub64, (double*)gwork, use_smem ? 1 : 0, 40,
         1e-13, info);
   } else {
     if (use_smem && smem > 48 * 1024)
       BGPU_CUDA(allow_max_smem(k_jacobi<float>));
-    k_jacobi<float><<<1, 1024, use_smem ? smem : 0, s>>>(
+    k_jacobi<float><<<1, threads, use_smem ? smem : 0, s>>>(
         Bf, m, Ub, Sb, Vbt, ub_last, sb64, ub64, (float*)gwork, use_smem ? 1 : 0, 40,
         jacobi_threshold(m), info);
   }

@@ -75,7 +75,9 @@ __global__ void k_build_tail(const double* __restrict__ B, uint32_t m, uint32_t 
   }
 }
 
-// Poles, sorted ascending, and deflation. One block.
+// Poles, sorted ascending, and deflation. One block; the sequential scan
+// works on shared-memory copies (a global round trip per step would cost
+// more than the rest of the merge).
 __global__ void __launch_bounds__(256)
 k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
               const double* __restrict__ Q, const double* __restrict__ sig_t,
@@ -83,6 +85,10 @@ k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
   extern __shared__ double sm[];
   double* d0 = sm;      // unsorted d
   double* z0 = d0 + m;  // unsorted z
+  double* ds = z0 + m;  // sorted
+  double* zs = ds + m;
+  int* src = reinterpret_cast<int*>(zs + m);
+  int* defl = src + m;
   const uint32_t t = m - kc;
   const double alpha = B[kc + (uint64_t)kc * m];
   for (uint32_t l = threadIdx.x; l < m; l += blockDim.x) {
@@ -104,65 +110,71 @@ k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
       const double dq = d0[q];
       rank += (dq < dl || (dq == dl && q < l)) ? 1u : 0u;
     }
-    w.ds[rank] = dl;
-    w.zs[rank] = z0[l];
-    w.src[rank] = (int)l;
+    ds[rank] = dl;
+    zs[rank] = z0[l];
+    src[rank] = (int)l;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  // one sequential O(m) scan: tolerance, then single-component and
-  // close-pole deflation in ascending order
-  double zn2 = 0.0, dmax = 0.0;
-  for (uint32_t l = 0; l < m; ++l) {
-    zn2 += w.zs[l] * w.zs[l];
-    dmax = fmax(dmax, fabs(w.ds[l]));
-  }
-  const double znrm = sqrt(zn2);
-  const double tol = 8.0 * kEps * fmax(dmax, zn2);
-  int nrot = 0, nnd = 0, ndef = 0;
-  int prev = -1;
-  for (uint32_t l = 0; l < m; ++l) {
-    if (fabs(w.zs[l]) * znrm <= tol) {
-      w.defl[l] = 1;
-      continue;
+  if (threadIdx.x == 0) {
+    // one sequential O(m) scan: tolerance, then single-component and
+    // close-pole deflation in ascending order
+    double zn2 = 0.0, dmax = 0.0;
+    for (uint32_t l = 0; l < m; ++l) {
+      zn2 += zs[l] * zs[l];
+      dmax = fmax(dmax, fabs(ds[l]));
     }
-    w.defl[l] = 0;
-    if (prev >= 0) {
-      const double zp = w.zs[prev], zq = w.zs[l];
-      const double r = hypot(zp, zq);
-      const double c = zq / r, sn = zp / r;
-      if (fabs((w.ds[l] - w.ds[prev]) * c * sn) <= tol) {
-        const double dp = w.ds[prev], dq = w.ds[l];
-        w.ds[prev] = dp * c * c + dq * sn * sn;
-        w.ds[l] = dp * sn * sn + dq * c * c;
-        w.zs[prev] = 0.0;
-        w.zs[l] = r;
-        w.defl[prev] = 1;
-        w.rot_p[nrot] = prev;
-        w.rot_q[nrot] = (int)l;
-        w.rot_c[nrot] = c;
-        w.rot_s[nrot] = sn;
-        ++nrot;
+    const double znrm = sqrt(zn2);
+    const double tol = 8.0 * kEps * fmax(dmax, zn2);
+    int nrot = 0, nnd = 0, ndef = 0;
+    int prev = -1;
+    for (uint32_t l = 0; l < m; ++l) {
+      if (fabs(zs[l]) * znrm <= tol) {
+        defl[l] = 1;
+        continue;
+      }
+      defl[l] = 0;
+      if (prev >= 0) {
+        const double zp = zs[prev], zq = zs[l];
+        const double r = hypot(zp, zq);
+        const double c = zq / r, sn = zp / r;
+        if (fabs((ds[l] - ds[prev]) * c * sn) <= tol) {
+          const double dp = ds[prev], dq = ds[l];
+          ds[prev] = dp * c * c + dq * sn * sn;
+          ds[l] = dp * sn * sn + dq * c * c;
+          zs[prev] = 0.0;
+          zs[l] = r;
+          defl[prev] = 1;
+          w.rot_p[nrot] = prev;
+          w.rot_q[nrot] = (int)l;
+          w.rot_c[nrot] = c;
+          w.rot_s[nrot] = sn;
+          ++nrot;
+        }
+      }
+      prev = (int)l;
+    }
+    double zz = 0.0;
+    for (uint32_t l = 0; l < m; ++l) {
+      if (defl[l]) {
+        w.defpos[ndef++] = (int)l;
+      } else {
+        w.ndpos[nnd] = (int)l;
+        w.dn[nnd] = ds[l];
+        w.zn[nnd] = zs[l];
+        zz += zs[l] * zs[l];
+        ++nnd;
       }
     }
-    prev = (int)l;
+    w.state[0] = nnd;
+    w.state[1] = nrot;
+    w.state[2] = ndef;
+    w.znorm2[0] = zz;
   }
-  double zz = 0.0;
-  for (uint32_t l = 0; l < m; ++l) {
-    if (w.defl[l]) {
-      w.defpos[ndef++] = (int)l;
-    } else {
-      w.ndpos[nnd] = (int)l;
-      w.dn[nnd] = w.ds[l];
-      w.zn[nnd] = w.zs[l];
-      zz += w.zs[l] * w.zs[l];
-      ++nnd;
-    }
+  __syncthreads();
+  for (uint32_t l = threadIdx.x; l < m; l += blockDim.x) {  // for the later kernels
+    w.ds[l] = ds[l];
+    w.src[l] = src[l];
   }
-  w.state[0] = nnd;
-  w.state[1] = nrot;
-  w.state[2] = ndef;
-  w.znorm2[0] = zz;
 }
 
 // Secular roots, one warp per root (grid m; blocks past n' return).
@@ -458,7 +470,8 @@ int launch_svd_merge(const double* B, uint32_t m, uint32_t kc, float* Ub, float*
                                refine_steps, s, Q64));
   }
   // 2. the merge
-  k_merge_setup<<<1, 256, (size_t)2 * m * 8, s>>>(B, m, kc, Q64, sb_t, w);
+  k_merge_setup<<<1, 256, (size_t)4 * m * 8 + (size_t)2 * m * 4, s>>>(B, m, kc, Q64,
+                                                                      sb_t, w);
   BGPU_CHECK_LAUNCH();
   k_merge_roots<<<m, 32, 0, s>>>(w);
   BGPU_CHECK_LAUNCH();
