@@ -319,9 +319,11 @@ k_knn_search(const float* __restrict__ X, uint64_t n, uint32_t d,
     for (uint64_t r0 = cb; r0 < ce; r0 += kCellTile) {
       const uint32_t tn = (uint32_t)(ce - r0 < (uint64_t)kCellTile ? ce - r0 : (uint64_t)kCellTile);
       __syncthreads();  // previous tile consumed
-      for (uint32_t t = threadIdx.x; t < (uint32_t)kCellTile * d; t += kKnnThreads) {
-        const uint32_t r = t / d, j = t % d;
-        if (r < tn) tile[(size_t)r * st + j] = X[(r0 + r) * d + j];
+      // rows past the cluster and the padding columns d..st are zeroed: the
+      // float4 dot reads them (times zero query entries)
+      for (uint32_t t = threadIdx.x; t < (uint32_t)kCellTile * st; t += kKnnThreads) {
+        const uint32_t r = t / st, j = t % st;
+        tile[t] = (r < tn && j < d) ? X[(r0 + r) * d + j] : 0.f;
       }
       for (uint32_t t = threadIdx.x; t < (uint32_t)kCellTile; t += kKnnThreads)
         tnorm[t] = t < tn ? norms[r0 + t] : 0.f;

@@ -36,11 +36,11 @@
 // coalesced 32-byte row runs into registers, split and written in the
 // canonical no-swizzle K-major layout (8-row x 16-byte core matrices of 8
 // BF16, K-direction core stride LBO = 128 B, 8-row stride SBO = Kp/8 * 128
-// B); one elected thread issues 6 * Kp/16 MMAs of M=128, N=Np, K=16 and
-// commits them to an mbarrier. The next tile's loads are issued right after
-// the MMAs, so they are in flight while the MMAs run and while all 16 warps
-// read the accumulator back (tcgen05.ld, 32 lanes x 8 columns per load) and
-// store C column-major (128-byte runs per column).
+// B); one elected thread issues 6 * Kp/16 MMAs of M=128, N=Np, K=16 into one
+// of two TMEM accumulators and commits them to that accumulator's mbarrier.
+// While they run, the next tile's loads are in flight and all 16 warps drain
+// the previous tile's accumulator (tcgen05.ld, 32 lanes x 8 columns per
+// load) and store C column-major (128-byte runs per column).
 //
 // Every mbarrier wait is bounded (about 1 s of SM clock): on timeout the
 // kernel records kDevErrTimeout, stops, frees its TMEM and returns.
@@ -194,7 +194,7 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
           uint32_t tmem_cols, int accumulate, const float* __restrict__ Apiv,
           const int* __restrict__ piv, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);  // two: one per accumulator
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
   __shared__ int stop;
   __shared__ int spiv[kTcChunkN];  // pivot of each output column (0: none)
@@ -205,12 +205,13 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
 
   if (wid == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_u32(tslot)), "r"(tmem_cols)
+                 ::"r"(smem_u32(tslot)), "r"(2u * tmem_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(bar, 1);
+    mbar_init(bars, 1);
+    mbar_init(bars + 1, 1);
     fence_mbar_init();
     stop = 0;
   }
@@ -257,61 +258,16 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   };
 
   const uint64_t ntiles = (rows + kTcRows - 1) / kTcRows;
-  uint32_t phase = 0;
-  uint64_t tile = blockIdx.x;
-  if (tile < ntiles) load_tile(tile * kTcRows);
-  for (; tile < ntiles; tile += gridDim.x) {
-    const uint64_t row0 = tile * kTcRows;
-#pragma unroll
-    for (int i = 0; i < kTcTasks; ++i) {
-      const uint32_t t = tid + i * kTcThreads;
-      if (t < ntask) {
-        const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
-        uint4 p[3];
-        split8(xa[i], p);
-#pragma unroll
-        for (int part = 0; part < 3; ++part)
-          *reinterpret_cast<uint4*>(smem + L.a[part] + core_off(rg * 8 + rr, kg, kq)) =
-              p[part];
-      }
-    }
-    fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      for (uint32_t ks = 0; ks < Kp / 16; ++ks) {
-        const uint32_t off = ks * 256u;  // two 16-byte K groups per K=16 step
-        uint64_t da[3], db[3];
-#pragma unroll
-        for (int part = 0; part < 3; ++part) {
-          da[part] = smem_desc(base + L.a[part] + off, 128u, sbo);
-          db[part] = smem_desc(base + L.b[part] + off, 128u, sbo);
-        }
-        // the small cross products first: x1y3 + x2y2 + x3y1 + x1y2 + x2y1
-        mma_bf16(tmem, da[0], db[2], idesc, ks > 0 ? 1u : 0u);
-        mma_bf16(tmem, da[1], db[1], idesc, 1u);
-        mma_bf16(tmem, da[2], db[0], idesc, 1u);
-        mma_bf16(tmem, da[0], db[1], idesc, 1u);
-        mma_bf16(tmem, da[1], db[0], idesc, 1u);
-      }
-      for (uint32_t ks = 0; ks < Kp / 16; ++ks) {  // then x1y1
-        const uint32_t off = ks * 256u;
-        mma_bf16(tmem, smem_desc(base + L.a[0] + off, 128u, sbo),
-                 smem_desc(base + L.b[0] + off, 128u, sbo), idesc, 1u);
-      }
-      mma_commit(bar);
-    }
-    // the next tile's loads fly while the MMAs run and the accumulator drains
-    if (tile + gridDim.x < ntiles) load_tile((tile + gridDim.x) * kTcRows);
-    // Epilogue mapping: warp w reads TMEM lanes 32*(w%4).. (tile rows) and
-    // the columns of quarter w/4 (<= 32 columns); lane = row. The pivot
-    // columns' FP32 values of this thread's row (L2-resident: the tile was
-    // just read) are fetched now, all in flight at once, signed.
-    const uint32_t q = wid & 3u, h = wid >> 2;
-    const uint32_t quarter = Np / 4;
+  // Two accumulators: the MMAs of tile i run while the epilogue of tile
+  // i - 1 drains the other one and the loads of tile i + 1 are in flight.
+  // Iteration it waits for the MMAs of it - 1 (which frees the shared A
+  // tile and completes that accumulator), stages and issues tile it, then
+  // drains tile it - 1.
+  const uint32_t q = wid & 3u, h = wid >> 2;
+  const uint32_t quarter = Np / 4;  // columns per epilogue warp (<= 32)
+  float pa[32];                     // signed pivot values of this thread's row
+  auto prefetch_pivots = [&](uint64_t row0) {
     const uint64_t gr = row0 + q * 32 + lane;
-    float pa[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       const uint32_t c = h * quarter + j;
@@ -323,19 +279,17 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
       }
       pa[j] = a;
     }
-    const bool ok = mbar_wait(bar, phase, err);
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) stop = 1;
-      break;
-    }
-    phase ^= 1u;
-    tc_fence_after();
+  };
+  // Epilogue: warp w reads TMEM lanes 32*(w%4).. (tile rows) and the columns
+  // of quarter w/4; lane = row.
+  auto epilogue = [&](uint64_t row0, uint32_t acc) {
+    const uint64_t gr = row0 + q * 32 + lane;
 #pragma unroll
     for (uint32_t g8 = 0; g8 < 4; ++g8) {
       const uint32_t c0 = h * quarter + g8 * 8;
       if (g8 * 8 >= quarter) break;
       float v[8];
-      tmem_ld8(tmem + ((q * 32u) << 16) + c0, v);
+      tmem_ld8(acc + ((q * 32u) << 16) + c0, v);
       if (gr < rows) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -347,19 +301,87 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
         }
       }
     }
-    tc_fence_before();
-    __syncthreads();  // TMEM read and smem A free before the next tile
+  };
+  uint32_t phases = 0u;  // bit b: the phase accumulator b's barrier waits for
+  int pend = -1;  // accumulator whose MMAs are committed and not yet waited for
+  uint64_t tile = blockIdx.x, prev = 0;
+  if (tile < ntiles) load_tile(tile * kTcRows);
+  for (uint32_t it = 0;; ++it) {
+    const bool has_cur = tile < ntiles;
+    if (it > 0) {  // the MMAs of tile `prev`
+      const uint32_t pb = (it - 1) & 1u;
+      const bool ok = mbar_wait(bars + pb, (phases >> pb) & 1u, err);
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) stop = 1;
+        break;
+      }
+      phases ^= 1u << pb;
+      pend = -1;
+      tc_fence_after();
+    }
+    if (has_cur) {
+#pragma unroll
+      for (int i = 0; i < kTcTasks; ++i) {
+        const uint32_t t = tid + i * kTcThreads;
+        if (t < ntask) {
+          const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
+          uint4 p[3];
+          split8(xa[i], p);
+#pragma unroll
+          for (int part = 0; part < 3; ++part)
+            *reinterpret_cast<uint4*>(smem + L.a[part] + core_off(rg * 8 + rr, kg, kq)) =
+                p[part];
+        }
+      }
+      fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
+      tc_fence_before();
+      __syncthreads();
+      const uint32_t acc = tmem + (it & 1u) * tmem_cols;
+      if (tid == 0) {
+        tc_fence_after();
+        for (uint32_t ks = 0; ks < Kp / 16; ++ks) {
+          const uint32_t off = ks * 256u;  // two 16-byte K groups per K=16 step
+          uint64_t da[3], db[3];
+#pragma unroll
+          for (int part = 0; part < 3; ++part) {
+            da[part] = smem_desc(base + L.a[part] + off, 128u, sbo);
+            db[part] = smem_desc(base + L.b[part] + off, 128u, sbo);
+          }
+          // the small cross products first: x1y3 + x2y2 + x3y1 + x1y2 + x2y1
+          mma_bf16(acc, da[0], db[2], idesc, ks > 0 ? 1u : 0u);
+          mma_bf16(acc, da[1], db[1], idesc, 1u);
+          mma_bf16(acc, da[2], db[0], idesc, 1u);
+          mma_bf16(acc, da[0], db[1], idesc, 1u);
+          mma_bf16(acc, da[1], db[0], idesc, 1u);
+        }
+        for (uint32_t ks = 0; ks < Kp / 16; ++ks) {  // then x1y1
+          const uint32_t off = ks * 256u;
+          mma_bf16(acc, smem_desc(base + L.a[0] + off, 128u, sbo),
+                   smem_desc(base + L.b[0] + off, 128u, sbo), idesc, 1u);
+        }
+        mma_commit(bars + (it & 1u));
+      }
+      pend = (int)(it & 1u);
+      // the next tile's loads fly while these MMAs run
+      if (tile + gridDim.x < ntiles) load_tile((tile + gridDim.x) * kTcRows);
+    }
+    if (it > 0) epilogue(prev * kTcRows, tmem + ((it - 1) & 1u) * tmem_cols);
+    if (!has_cur) break;
+    prefetch_pivots(tile * kTcRows);  // for this tile's epilogue
+    tc_fence_before();  // the epilogue's TMEM reads before the next barrier
+    prev = tile;
+    tile += gridDim.x;
   }
   __syncthreads();
-  if (stop) {
-    // the timed-out commit may still be outstanding: give it one more bounded
-    // wait before the TMEM goes back
-    (void)mbar_wait(bar, phase, nullptr);
+  if (stop && pend >= 0) {
+    // a committed group may still be outstanding: one more bounded wait
+    // before the TMEM goes back
+    (void)mbar_wait(bars + pend, (phases >> pend) & 1u, nullptr);
   }
   tc_fence_after();
   if (wid == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                 ::"r"(tmem), "r"(tmem_cols)
+                 ::"r"(tmem), "r"(2u * tmem_cols)
                  : "memory");
   }
 }
@@ -379,6 +401,8 @@ static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t
   const uint32_t Kp = (K + 15) & ~15u, Np = (ncols + 31) & ~31u;
   uint32_t tcols = 32;
   while (tcols < Np) tcols <<= 1;
+  BGPU_REQUIRE(2 * tcols <= 512, BGPU_ERR_UNSUPPORTED,
+               "tensor-core rotation: two accumulators must fit the 512 TMEM columns");
   // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM
   const size_t smem = std::max<size_t>(TcLayout(Kp, Np).total, 120 * 1024);
   BGPU_CUDA(allow_max_smem(k_gemm_tc));
