@@ -135,6 +135,8 @@ SIGNATURES = {
     "bgpu_clipped_sum": (_i, [C.POINTER(HvgInput), _u64, _vp, _vp, _vp, _vp]),
     "bgpu_knn_self": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64, _u32,
                            _u32, _u32, _u32, _vp]),
+    "bgpu_kmeans": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _u32, _f, _u32, _u64,
+                         _u64, _u32, _u32, C.POINTER(_u32), _vp]),
 }
 
 _lock = threading.Lock()

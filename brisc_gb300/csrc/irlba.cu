@@ -22,6 +22,7 @@
 
 #include "dense.cuh"
 #include "matrix.cuh"
+#include "pcg.h"
 #include "svd.cuh"
 
 namespace bgpu {
@@ -70,24 +71,6 @@ int device_smem_optin() {
 // PCG32 + Box-Muller start vector, restating brisc/cyutils.pyx:1153-1232 and
 // brisc/pca.pyx:801-806 operation for operation (float arithmetic as there).
 namespace {
-
-inline uint32_t pcg_rand(uint64_t* state) {  // cyutils.pyx:1153-1158
-  const uint64_t x = *state;
-  *state = x * 6364136223846793005ULL + 1442695040888963407ULL;
-  const uint32_t s = (uint32_t)((x ^ (x >> 18)) >> 27);
-  const uint32_t rot = (uint32_t)(x >> 59);
-  return (s >> rot) | (s << ((0u - rot) & 31u));
-}
-
-inline uint64_t pcg_srand(uint64_t seed) {  // cyutils.pyx:1228-1232
-  uint64_t state = seed + 1442695040888963407ULL;
-  pcg_rand(&state);
-  return state;
-}
-
-inline float pcg_uniform(uint64_t* state) {  // cyutils.pyx:1175-1177
-  return (float)pcg_rand(state) / (float)4294967295u;
-}
 
 inline float pcg_normal(uint64_t* state) {  // cyutils.pyx:1180-1191
   float u1;

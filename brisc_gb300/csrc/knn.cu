@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "pcg.h"
 
 namespace bgpu {
 
@@ -493,6 +494,288 @@ extern "C" int bgpu_knn_self(const float* X, const uint32_t* sorted_order,
   }
   cudaFreeAsync(cn, s);
   cudaFreeAsync(coff, s);
+  if (rc == BGPU_OK) BGPU_CUDA(cudaStreamSynchronize(s));
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// k-means: the reference's kmeans (brisc/kmeans.pyx:889-1433), random
+// initialisation (its default, kmeans_random_init, kmeans.pyx:13-38), for
+// neighbors() to cluster the PCs on the device before knn_self.
+//  - init: num_clusters distinct random cells, drawn with PCG32 + Lemire's
+//    bounded integers from srand(seed) exactly as the reference draws them
+//    (host), gathered on the device;
+//  - |x|^2 per cell (kmeans.pyx:954-965), a dimension-ordered float sum;
+//  - E step: the nearest centroid by partial distance |c|^2 - 2 x.c, first
+//    minimum in centroid order wins (kmeans.pyx:1016-1041) -- k_knn_nearest
+//    with one cluster searched;
+//  - M step: the sums of each chunk of chunk_size cells per cluster, each a
+//    sequence over the chunk's cells in order, then the chunks added in
+//    chunk order (kmeans.pyx:1043-1064): the reference's own order, so with
+//    the same assignments the centroids are bit-identical; empty clusters
+//    take the cells farthest from their centroids (kmeans.pyx:747-820, on
+//    the host: it is rare and sequential); the sums are scaled by
+//    (float)(1.0 / count);
+//  - stop after num_kmeans_iterations, or when the float total of |x|^2 +
+//    min distance falls by less than tolerance (kmeans.pyx:1082-1098, summed
+//    in cell order on the host);
+//  - a final E step for the labels, min distances and counts.
+// The centroid buffers swap every iteration as the reference's do: the
+// final centroids are in centroids_new when the returned count is odd.
+namespace bgpu {
+namespace {
+
+__global__ void k_km_cell_norms(const float* __restrict__ X, uint64_t n, uint32_t d,
+                                float* __restrict__ out) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* x = X + i * d;
+  float s = x[0] * x[0];
+  for (uint32_t j = 1; j < d; ++j) s = fmaf(x[j], x[j], s);
+  out[i] = s;
+}
+
+__global__ void k_km_gather(const float* __restrict__ X, const uint32_t* __restrict__ idx,
+                            uint32_t nc, uint32_t d, float* __restrict__ C) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)nc * d) return;
+  const uint32_t c = (uint32_t)(t / d), j = (uint32_t)(t % d);
+  C[t] = X[(uint64_t)idx[c] * d + j];
+}
+
+// One CTA per chunk, one thread per dimension: sums[chunk][label][dim] over
+// the chunk's cells in order (zeroed beforehand).
+__global__ void k_km_chunk_sums(const float* __restrict__ X, uint64_t n, uint32_t d,
+                                const uint32_t* __restrict__ labels, uint32_t chunk,
+                                uint32_t nc, float* __restrict__ sums) {
+  const uint64_t c0 = (uint64_t)blockIdx.x * chunk;
+  const uint64_t c1 = c0 + chunk < n ? c0 + chunk : n;
+  float* base = sums + (uint64_t)blockIdx.x * nc * d;
+  for (uint32_t j = threadIdx.x; j < d; j += blockDim.x)
+    for (uint64_t i = c0; i < c1; ++i) {
+      float* p = base + (uint64_t)labels[i] * d + j;
+      *p = *p + X[i * d + j];
+    }
+}
+
+// centroids_new[c][j] = 0 + the chunk sums in chunk order.
+__global__ void k_km_reduce(const float* __restrict__ sums, uint32_t nchunks, uint32_t nc,
+                            uint32_t d, float* __restrict__ Cn) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t per = (uint64_t)nc * d;
+  if (t >= per) return;
+  float s = 0.f;
+  for (uint32_t ch = 0; ch < nchunks; ++ch) s += sums[ch * per + t];
+  Cn[t] = s;
+}
+
+__global__ void k_km_counts(const uint32_t* __restrict__ labels, uint64_t n,
+                            uint32_t* __restrict__ counts) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&counts[labels[i]], 1u);  // integer: order-free
+}
+
+__global__ void k_km_normalize(float* __restrict__ Cn, const uint32_t* __restrict__ counts,
+                               uint32_t nc, uint32_t d) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)nc * d) return;
+  const uint32_t cnt = counts[t / d];
+  if (cnt > 0) Cn[t] *= (float)(1.0 / (double)cnt);  // kmeans.pyx:1070-1074
+}
+
+// Squared distance of each cell to its assigned centroid, a dimension-ordered
+// float sum (relocate_empty_clusters, kmeans.pyx:785-791).
+__global__ void k_km_assigned(const float* __restrict__ X, const uint32_t* __restrict__ lab,
+                              const float* __restrict__ C, uint64_t n, uint32_t d,
+                              float* __restrict__ out) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* x = X + i * d;
+  const float* c = C + (uint64_t)lab[i] * d;
+  float diff = x[0] - c[0];
+  float s = diff * diff;
+  for (uint32_t j = 1; j < d; ++j) {
+    diff = x[j] - c[j];
+    s = fmaf(diff, diff, s);
+  }
+  out[i] = s;
+}
+
+// E step: labels, min distances (= partial distances) and, when counts is
+// given, the cluster sizes.
+int km_estep(const float* X, uint64_t n, uint32_t d, const float* C, float* cn,
+             uint32_t nc, uint32_t* labels, float* mind, uint32_t* counts, cudaStream_t s) {
+  k_knn_centroid_norms<<<(unsigned)ceil_div(nc, 256), 256, 0, s>>>(C, nc, d, cn);
+  BGPU_CHECK_LAUNCH();
+  BGPU_TRY(launch_nearest<1>(X, n, d, C, cn, nc, 1, labels, mind, s));
+  if (counts) {
+    BGPU_CUDA(cudaMemsetAsync(counts, 0, (size_t)nc * 4, s));
+    k_km_counts<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(labels, n, counts);
+    BGPU_CHECK_LAUNCH();
+  }
+  return BGPU_OK;
+}
+
+// Float sum of the values in order, starting from init (host; the
+// reference's sequential loops).
+float seq_sum(float init, const std::vector<float>& v) {
+  float t = init;
+  for (float x : v) t += x;
+  return t;
+}
+
+}  // namespace
+}  // namespace bgpu
+
+extern "C" int bgpu_kmeans(const float* X, uint32_t* cluster_labels, float* centroids,
+                           float* centroids_new, uint32_t* num_cells_per_cluster,
+                           float* min_distances, float* cell_norms, int kmeans_barbar,
+                           uint32_t num_kmeans_iterations, float tolerance,
+                           uint32_t chunk_size, uint64_t seed, uint64_t num_cells,
+                           uint32_t num_dimensions, uint32_t num_clusters,
+                           uint32_t* iterations, void* stream) {
+  BGPU_REQUIRE(X && cluster_labels && centroids && centroids_new && num_cells_per_cluster &&
+                   min_distances && iterations,
+               BGPU_ERR_INVALID, "kmeans: NULL argument");
+  BGPU_REQUIRE(!kmeans_barbar, BGPU_ERR_UNSUPPORTED,
+               "kmeans: only the random initialisation (kmeans_barbar=False, the "
+               "reference's default) runs on the GPU");
+  const uint64_t n = num_cells;
+  const uint32_t d = num_dimensions, nc = num_clusters;
+  BGPU_REQUIRE(n >= 1 && d >= 1 && nc >= 1 && nc <= n, BGPU_ERR_INVALID,
+               "kmeans: needs 1 <= num_clusters <= num_cells and >= 1 dimension");
+  BGPU_REQUIRE(d <= kMaxDims, BGPU_ERR_UNSUPPORTED, "kmeans: at most 128 dimensions");
+  BGPU_REQUIRE(nc <= kMaxClusters, BGPU_ERR_UNSUPPORTED, "kmeans: at most 32768 clusters");
+  BGPU_REQUIRE(chunk_size >= 1 && num_kmeans_iterations >= 1, BGPU_ERR_INVALID,
+               "kmeans: chunk_size and num_kmeans_iterations must be >= 1");
+  BGPU_REQUIRE(n <= 0xFFFFFFFFull, BGPU_ERR_UNSUPPORTED, "kmeans: at most 2^32 - 1 cells");
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t nchunks = (uint32_t)ceil_div(n, chunk_size);
+  const uint64_t per = (uint64_t)nc * d;
+  const uint64_t sums_bytes = (uint64_t)nchunks * per * 4;
+  BGPU_REQUIRE(sums_bytes <= (64ull << 30), BGPU_ERR_UNSUPPORTED,
+               "kmeans: the per-chunk sums would exceed 64 GB; raise chunk_size");
+
+  // random initialisation (kmeans.pyx:13-38)
+  std::vector<uint32_t> init(nc);
+  {
+    std::vector<uint64_t> bits((n + 63) / 64, 0);
+    uint64_t state = pcg_srand(seed);
+    for (uint32_t i = 0; i < nc; ++i) {
+      while (true) {
+        const uint32_t j = pcg_randint((uint32_t)n, &state);
+        if (!(bits[j >> 6] & (1ull << (j & 63)))) {
+          bits[j >> 6] |= 1ull << (j & 63);
+          init[i] = j;
+          break;
+        }
+      }
+    }
+  }
+  uint32_t* didx = nullptr;
+  float *cn = nullptr, *sums = nullptr, *norms = cell_norms, *own_norms = nullptr;
+  BGPU_CUDA(cudaMallocAsync((void**)&didx, (size_t)nc * 4, s));
+  BGPU_CUDA(cudaMallocAsync((void**)&cn, (size_t)nc * 4, s));
+  BGPU_CUDA(cudaMallocAsync((void**)&sums, sums_bytes, s));
+  if (!norms) {
+    BGPU_CUDA(cudaMallocAsync((void**)&own_norms, n * 4, s));
+    norms = own_norms;
+  }
+  auto cleanup = [&]() {
+    cudaFreeAsync(didx, s);
+    cudaFreeAsync(cn, s);
+    cudaFreeAsync(sums, s);
+    if (own_norms) cudaFreeAsync(own_norms, s);
+  };
+  auto run = [&]() -> int {
+    BGPU_CUDA(cudaMemcpyAsync(didx, init.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, s));
+    float* Cc = centroids;
+    float* Cn = centroids_new;
+    k_km_gather<<<(unsigned)ceil_div(per, 256), 256, 0, s>>>(X, didx, nc, d, Cc);
+    BGPU_CHECK_LAUNCH();
+    k_km_cell_norms<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(X, n, d, norms);
+    BGPU_CHECK_LAUNCH();
+    std::vector<float> hnorm(n), hmin;
+    BGPU_CUDA(cudaMemcpyAsync(hnorm.data(), norms, n * 4, cudaMemcpyDeviceToHost, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));
+    const float sum_sq = seq_sum(0.f, hnorm);  // kmeans.pyx:954-965
+    float old_total = 0.f;
+    uint32_t it = 0;
+    std::vector<uint32_t> hcount(nc);
+    while (true) {
+      BGPU_TRY(km_estep(X, n, d, Cc, cn, nc, cluster_labels, min_distances,
+                        num_cells_per_cluster, s));
+      BGPU_CUDA(cudaMemsetAsync(sums, 0, sums_bytes, s));
+      k_km_chunk_sums<<<nchunks, std::min<uint32_t>(128, (d + 31) & ~31u), 0, s>>>(
+          X, n, d, cluster_labels, chunk_size, nc, sums);
+      BGPU_CHECK_LAUNCH();
+      k_km_reduce<<<(unsigned)ceil_div(per, 256), 256, 0, s>>>(sums, nchunks, nc, d, Cn);
+      BGPU_CHECK_LAUNCH();
+      BGPU_CUDA(cudaMemcpyAsync(hcount.data(), num_cells_per_cluster, (size_t)nc * 4,
+                                cudaMemcpyDeviceToHost, s));
+      BGPU_CUDA(cudaStreamSynchronize(s));
+      std::vector<uint32_t> empty;
+      for (uint32_t c = 0; c < nc; ++c)
+        if (hcount[c] == 0) empty.push_back(c);
+      if (!empty.empty()) {  // relocate_empty_clusters (kmeans.pyx:747-820)
+        float* dist = nullptr;
+        BGPU_CUDA(cudaMallocAsync((void**)&dist, n * 4, s));
+        k_km_assigned<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(X, cluster_labels, Cc,
+                                                                  n, d, dist);
+        std::vector<float> hd(n), hx, hcn(per);
+        std::vector<uint32_t> hl(n);
+        cudaMemcpyAsync(hd.data(), dist, n * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hl.data(), cluster_labels, n * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hcn.data(), Cn, per * 4, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(dist, s);
+        BGPU_CUDA(cudaStreamSynchronize(s));
+        // the num_empty largest distances, an earlier cell winning ties, in
+        // descending order
+        const size_t ne = empty.size();
+        std::vector<uint64_t> order(n);
+        for (uint64_t i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](uint64_t a, uint64_t b) { return hd[a] > hd[b]; });
+        BGPU_REQUIRE(hd[order[0]] != 0.f, BGPU_ERR_INVALID,
+                     "kmeans: num_clusters is greater than the number of cells with "
+                     "distinct principal component loadings; decrease num_clusters");
+        std::vector<float> row(d);
+        for (size_t e = 0; e < ne; ++e) {
+          const uint64_t j = order[e];
+          const uint32_t oldc = hl[j], newc = empty[e];
+          BGPU_CUDA(cudaMemcpy(row.data(), X + j * d, (size_t)d * 4, cudaMemcpyDeviceToHost));
+          for (uint32_t k = 0; k < d; ++k) {
+            hcn[(uint64_t)oldc * d + k] -= row[k];
+            hcn[(uint64_t)newc * d + k] = row[k];
+          }
+          hcount[oldc] -= 1;
+          hcount[newc] += 1;
+        }
+        BGPU_CUDA(cudaMemcpyAsync(Cn, hcn.data(), per * 4, cudaMemcpyHostToDevice, s));
+        BGPU_CUDA(cudaMemcpyAsync(num_cells_per_cluster, hcount.data(), (size_t)nc * 4,
+                                  cudaMemcpyHostToDevice, s));
+      }
+      k_km_normalize<<<(unsigned)ceil_div(per, 256), 256, 0, s>>>(Cn, num_cells_per_cluster,
+                                                                  nc, d);
+      BGPU_CHECK_LAUNCH();
+      std::swap(Cc, Cn);
+      ++it;
+      if (it == num_kmeans_iterations) break;
+      hmin.resize(n);
+      BGPU_CUDA(cudaMemcpyAsync(hmin.data(), min_distances, n * 4, cudaMemcpyDeviceToHost, s));
+      BGPU_CUDA(cudaStreamSynchronize(s));
+      const float total = seq_sum(sum_sq, hmin);  // kmeans.pyx:1088-1098
+      if (it > 1 && old_total - total < tolerance * old_total) break;
+      old_total = total;
+    }
+    // the final E step (kmeans.pyx:1100-1153)
+    BGPU_TRY(km_estep(X, n, d, Cc, cn, nc, cluster_labels, min_distances,
+                      num_cells_per_cluster, s));
+    *iterations = it;
+    return BGPU_OK;
+  };
+  const int rc = run();
+  cleanup();
   if (rc == BGPU_OK) BGPU_CUDA(cudaStreamSynchronize(s));
   return rc;
 }

@@ -379,6 +379,27 @@ BGPU_API int bgpu_knn_self(const float* X, const uint32_t* sorted_order,
                            uint32_t num_clusters, uint32_t num_neighbors,
                            uint32_t num_clusters_searched, void* stream);
 
+/* kmeans (brisc/kmeans.pyx:889-1433, called by SingleCell.neighbors at
+ * brisc/single_cell.py:12532-12545), random initialisation only (the
+ * reference's default; kmeans_barbar must be 0, else BGPU_ERR_UNSUPPORTED).
+ * X: num_cells x num_dimensions row-major float32. Outputs: cluster_labels
+ * (uint32 per cell), centroids and centroids_new (num_clusters x
+ * num_dimensions; they swap every iteration, so the final centroids are in
+ * centroids_new when *iterations is odd, as in the reference),
+ * num_cells_per_cluster, min_distances (the partial distance |c|^2 - 2 x.c
+ * to the assigned centroid) and, when not NULL, cell_norms (|x|^2). The
+ * M step sums chunk_size cells at a time, in the reference's order.
+ * num_init_iterations and oversampling_factor belong to k-means|| and are
+ * not taken. Device pointers; synchronous. Limits: 128 dimensions, 32768
+ * clusters. */
+BGPU_API int bgpu_kmeans(const float* X, uint32_t* cluster_labels, float* centroids,
+                         float* centroids_new, uint32_t* num_cells_per_cluster,
+                         float* min_distances, float* cell_norms, int kmeans_barbar,
+                         uint32_t num_kmeans_iterations, float tolerance,
+                         uint32_t chunk_size, uint64_t seed, uint64_t num_cells,
+                         uint32_t num_dimensions, uint32_t num_clusters,
+                         uint32_t* iterations, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

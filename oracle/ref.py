@@ -156,9 +156,8 @@ def run_kmeans_for_knn(PCs, num_neighbors: int = 20, num_clusters=None,
     the argument preparation of brisc/single_cell.py:12451-12611 -- default
     cluster counts and chunk sizes, empty-cluster removal, the minimum number
     of clusters searched, centroids ordered by PC 1, cells sorted by cluster.
-    Returns every input knn_self (brisc/knn.pyx:13) takes, as a dict."""
-    M = load()
-    kmeans = M["kmeans"].kmeans
+    Returns every input knn_self (brisc/knn.pyx:13) takes, as a dict, plus
+    the raw kmeans outputs under "kmeans"."""
     X = np.ascontiguousarray(PCs, dtype=np.float32)
     num_threads = num_threads or os.cpu_count() or 1
     n, d = X.shape
@@ -170,23 +169,14 @@ def run_kmeans_for_knn(PCs, num_neighbors: int = 20, num_clusters=None,
         chunk_size_kmeans = min(4096, n)
     if chunk_size_search is None:
         chunk_size_search = min(256, n)
-    labels = np.zeros(n, dtype=np.uint32)
-    min_distances = np.zeros(n, dtype=np.float32)
-    cell_norms = np.zeros(n, dtype=np.float32)
-    centroids = np.empty((num_clusters, d), dtype=np.float32)
-    centroids_new = np.empty((num_clusters, d), dtype=np.float32)
-    counts = np.empty(num_clusters, dtype=np.uint32)
-    with _blas1():
-        it = kmeans(X=X, cluster_labels=labels, centroids=centroids,
-                    centroids_new=centroids_new, num_cells_per_cluster=counts,
-                    min_distances=min_distances, cell_norms=cell_norms,
-                    kmeans_barbar=kmeans_barbar,
-                    num_init_iterations=num_init_iterations,
-                    num_kmeans_iterations=num_kmeans_iterations,
-                    tolerance=kmeans_tolerance,
-                    oversampling_factor=oversampling_factor, seed=seed,
-                    chunk_size=chunk_size_kmeans, is_mac=False,
-                    num_threads=num_threads)
+    raw = run_kmeans(X, num_clusters, num_kmeans_iterations=num_kmeans_iterations,
+                     kmeans_tolerance=kmeans_tolerance, kmeans_barbar=kmeans_barbar,
+                     num_init_iterations=num_init_iterations,
+                     oversampling_factor=oversampling_factor,
+                     chunk_size=chunk_size_kmeans, seed=seed, num_threads=num_threads)
+    it, labels, centroids, centroids_new, counts, cell_norms = (
+        raw["iterations"], raw["cluster_labels"].copy(), raw["centroids"],
+        raw["centroids_new"], raw["num_cells_per_cluster"].copy(), raw["cell_norms"])
     if it & 1:
         centroids = centroids_new
     non_empty = counts > 0
@@ -213,7 +203,37 @@ def run_kmeans_for_knn(PCs, num_neighbors: int = 20, num_clusters=None,
                 num_neighbors=int(num_neighbors),
                 num_clusters_searched=int(num_clusters_searched),
                 chunk_size_kmeans=int(chunk_size_kmeans),
-                chunk_size_search=int(chunk_size_search))
+                chunk_size_search=int(chunk_size_search), kmeans=raw)
+
+
+def run_kmeans(X, num_clusters: int, num_kmeans_iterations: int = 2,
+               kmeans_tolerance: float = 1e-2, kmeans_barbar: bool = False,
+               num_init_iterations: int = 5, oversampling_factor: float = 1,
+               chunk_size: int | None = None, seed: int = 0,
+               num_threads: int | None = None) -> dict:
+    """The reference's compiled kmeans (brisc/kmeans.pyx:889) called as
+    neighbors() calls it (brisc/single_cell.py:12515-12545). Returns its raw
+    outputs: iterations, cluster_labels, centroids, centroids_new (the final
+    centroids are in centroids_new when iterations is odd), the cluster
+    sizes, min_distances and cell_norms."""
+    M = load()
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    n, d = X.shape
+    num_threads = num_threads or os.cpu_count() or 1
+    chunk_size = chunk_size or min(4096, n)
+    out = dict(cluster_labels=np.zeros(n, dtype=np.uint32),
+               min_distances=np.zeros(n, dtype=np.float32),
+               cell_norms=np.zeros(n, dtype=np.float32),
+               centroids=np.empty((num_clusters, d), dtype=np.float32),
+               centroids_new=np.empty((num_clusters, d), dtype=np.float32),
+               num_cells_per_cluster=np.empty(num_clusters, dtype=np.uint32))
+    with _blas1():
+        out["iterations"] = int(M["kmeans"].kmeans(
+            X=X, kmeans_barbar=kmeans_barbar, num_init_iterations=num_init_iterations,
+            num_kmeans_iterations=num_kmeans_iterations, tolerance=kmeans_tolerance,
+            oversampling_factor=oversampling_factor, seed=seed, chunk_size=chunk_size,
+            is_mac=False, num_threads=num_threads, **out))
+    return out
 
 
 def run_knn_self(prep: dict, num_threads: int | None = None):

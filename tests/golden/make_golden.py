@@ -18,8 +18,9 @@ reference's outputs, so the tests never regenerate data:
                  FP64 from the reference's PCs), the convergence flag, the
                  reference's own accuracy against the FP64 oracle, and a
                  fingerprint of the seeded input.
-* knn.npz        knn_self (brisc/knn.pyx:13) after the reference's kmeans
-                 (brisc/kmeans.pyx:889) and neighbors()'s argument
+* knn.npz        the reference's kmeans (brisc/kmeans.pyx:889; labels, final
+                 centroids, sizes, min distances, iterations) and knn_self
+                 (brisc/knn.pyx:13) after neighbors()'s argument
                  preparation (brisc/single_cell.py:12451-12611), on seeded
                  Gaussian-mixture "PCs" (regenerated from the seed, with a
                  fingerprint): the k-means outputs knn_self takes and its
@@ -147,6 +148,12 @@ def make_knn() -> None:
         out[f"{name}_fingerprint"] = np.array(hashlib.sha256(X.tobytes()).hexdigest())
         for key in ("sorted_order", "centroids", "num_cells_per_cluster", "cell_norms"):
             out[f"{name}_{key}"] = prep[key]
+        km = prep["kmeans"]
+        out[f"{name}_km_iterations"] = np.array(km["iterations"])
+        for key in ("cluster_labels", "num_cells_per_cluster", "min_distances"):
+            out[f"{name}_km_{key}"] = km[key]
+        out[f"{name}_km_final_centroids"] = (km["centroids_new"] if km["iterations"] & 1
+                                             else km["centroids"])
         out[f"{name}_neighbors"] = nbr
         out[f"{name}_distances"] = dist
         out[f"{name}_nearest_clusters"] = near

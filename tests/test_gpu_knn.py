@@ -106,3 +106,59 @@ def test_knn_self_matches_oracle(cuda, n, d, nc, k, cs):
     o = _run(c)
     check_against(c, o["neighbors"], o["distances"], o["nearest_clusters"],
                   o["centroid_distances"])
+
+
+@pytest.mark.parametrize("name", ["knn_a", "knn_b"])
+def test_kmeans_matches_reference(cuda, golden, name):
+    """GPU k-means (random initialisation, the reference's M-step order)
+    against the reference's kmeans on the same PCs: the same iteration count,
+    labels identical except at FP32 near-ties of the E step, centroids and
+    cluster sizes accordingly."""
+    from brisc_gb300 import knn
+    from knn_cases import knn_pcs
+    z = golden("knn")
+    n, d, comps, seed, k, cs = (int(v) for v in z[f"{name}_shape"])
+    X = knn_pcs(n, d, comps, seed)
+    ref_c = z[f"{name}_km_final_centroids"]
+    nc = ref_c.shape[0]
+    out = dict(cluster_labels=np.zeros(n, np.uint32), min_distances=np.zeros(n, np.float32),
+               cell_norms=np.zeros(n, np.float32),
+               centroids=np.zeros((nc, d), np.float32),
+               centroids_new=np.zeros((nc, d), np.float32),
+               num_cells_per_cluster=np.zeros(nc, np.uint32))
+    it = knn.kmeans(X=X, seed=0, chunk_size=min(4096, n), **out)
+    assert it == int(z[f"{name}_km_iterations"])
+    C = out["centroids_new"] if it & 1 else out["centroids"]
+    same = (out["cluster_labels"] == z[f"{name}_km_cluster_labels"]).mean()
+    assert same >= 0.999, same
+    scale = np.abs(ref_c).max()
+    if same == 1.0:  # same assignments: the reference's summation order
+        np.testing.assert_allclose(C, ref_c, rtol=0, atol=2e-6 * scale)
+        np.testing.assert_array_equal(out["num_cells_per_cluster"],
+                                      z[f"{name}_km_num_cells_per_cluster"])
+    else:
+        np.testing.assert_allclose(C, ref_c, rtol=0, atol=1e-2 * scale)
+    np.testing.assert_allclose(out["cell_norms"], z[f"{name}_cell_norms"][
+        np.argsort(z[f"{name}_sorted_order"])], rtol=2e-6)
+
+
+@pytest.mark.parametrize("name", ["knn_a", "knn_b"])
+def test_neighbors_pipeline_matches_reference(cuda, golden, name):
+    """brisc_gb300.knn.neighbors (GPU k-means, neighbors()'s preparation, GPU
+    knn_self) against the reference's neighbours, both in the original cell
+    order: the same sets except at near-ties."""
+    from brisc_gb300 import knn
+    from knn_cases import knn_pcs
+    from oracle import knn as oknn
+    z = golden("knn")
+    n, d, comps, seed, k, cs = (int(v) for v in z[f"{name}_shape"])
+    X = knn_pcs(n, d, comps, seed)
+    so = z[f"{name}_sorted_order"]
+    ref = np.empty_like(z[f"{name}_neighbors"])
+    ref[so] = z[f"{name}_neighbors"]
+    nbr, dist = knn.neighbors(X, num_neighbors=k,
+                              num_clusters_searched=None if name == "knn_b" else cs)
+    ident = np.arange(n, dtype=np.uint32)
+    norms = np.einsum("ij,ij->i", X, X).astype(np.float32)
+    same, worst = oknn.compare(X, ident, norms, nbr, ref)
+    assert same >= 0.99 and worst <= 1.0, (same, worst)
