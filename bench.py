@@ -902,6 +902,30 @@ def run_knn(args):
     e2e = (time.perf_counter() - t0) / e2e_steps
     same_paths = bool(np.array_equal(hn, gpu_nbr))
 
+    # k-means (the other half of neighbors()): the GPU's on device-resident
+    # PCs against the reference's run above, same seed and cluster count
+    nck = len(prep["kmeans"]["centroids"])
+    kX = torch.from_numpy(X).to(dev)
+    kout = dict(cluster_labels=torch.zeros(n, dtype=torch.int32, device=dev),
+                min_distances=torch.zeros(n, dtype=torch.float32, device=dev),
+                cell_norms=torch.zeros(n, dtype=torch.float32, device=dev),
+                centroids=torch.zeros((nck, d), dtype=torch.float32, device=dev),
+                centroids_new=torch.zeros((nck, d), dtype=torch.float32, device=dev),
+                num_cells_per_cluster=torch.zeros(nck, dtype=torch.int32, device=dev))
+    knn.kmeans(X=kX, seed=0, **kout)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    km_it = knn.kmeans(X=kX, seed=0, **kout)
+    torch.cuda.synchronize()
+    t_km_gpu = time.perf_counter() - t0
+    km_same = float((kout["cluster_labels"].cpu().numpy().view(np.uint32) ==
+                     prep["kmeans"]["cluster_labels"]).mean())
+    kmeans_block = {"gpu_seconds": t_km_gpu, "reference_seconds": t_kmeans,
+                    "reference_cores": cores, "iterations": km_it,
+                    "reference_iterations": prep["kmeans"]["iterations"],
+                    "labels_identical": km_same}
+    del kX, kout
+
     # candidate FLOPs: n C d for the nearest clusters, sum of searched
     # cluster sizes x d for the neighbour search (2 flop per multiply-add)
     near = hnc.astype(np.int64)
@@ -938,7 +962,7 @@ def run_knn(args):
                         "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz)",
                         "traffic": None, "flops_per_step": flops},
            "cpu_baseline": cpu, "agreement_with_reference": parity,
-           "host_and_device_paths_identical": same_paths,
+           "host_and_device_paths_identical": same_paths, "kmeans": kmeans_block,
            "clocks": clk.summary(), "gpu_launches": 4 * args.steps}
     print(json.dumps(out))
     return 0
