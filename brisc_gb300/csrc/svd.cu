@@ -249,7 +249,8 @@ k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
                 float* __restrict__ ratios) {
   __shared__ double red[8];
   __shared__ double rn_s;
-  __shared__ int conv_s, kc_s;
+  __shared__ int conv_s, kc_s, nconv_w[8];
+  __shared__ float smax_s;
   double t = 0.0;
   for (uint32_t c = threadIdx.x; c < g; c += blockDim.x) t += (double)rem[c] * rem[c];
   t = warp_sum(t);
@@ -258,17 +259,30 @@ k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < 8; ++w) s += red[w];
-    const double rn = sqrt(s);            // remainder_norm, pca.pyx:1181
-    const float S = fmaxf(Sb[0], *smax);  // pca.pyx:1187
-    *smax = S;
+    rn_s = sqrt(s);                          // remainder_norm, pca.pyx:1181
+    smax_s = fmaxf(Sb[0], *smax);            // pca.pyx:1187
+  }
+  __syncthreads();
+  // the residual test of every Ritz value at once (pca.pyx:1190-1193); the
+  // count is an integer sum, so its order does not matter
+  const double rn = rn_s;
+  const float S = smax_s;
+  uint32_t mine = 0;
+  for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
+    const double u = ub_last ? ub_last[i] : (double)Ub[(m - 1) + (uint64_t)i * m];
+    const double residual = fabs(rn * u);
+    const double bound = (double)tol * (double)S;
+    mine += residual < bound ? 1u : 0u;
+    if (ratios) ratios[i] = (float)(residual / bound);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if ((threadIdx.x & 31) == 0) nconv_w[threadIdx.x >> 5] = (int)mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
     uint32_t nconv = 0;
-    for (uint32_t i = 0; i < k; ++i) {    // pca.pyx:1190-1193
-      const double u = ub_last ? ub_last[i] : (double)Ub[(m - 1) + (uint64_t)i * m];
-      const double residual = fabs(rn * u);
-      const double bound = (double)tol * (double)S;
-      nconv += residual < bound ? 1u : 0u;
-      if (ratios) ratios[i] = (float)(residual / bound);
-    }
+    for (int w = 0; w < 8; ++w) nconv += (uint32_t)nconv_w[w];
+    *smax = S;
     const int conv = nconv == k;
     uint32_t kc_new = max(kc, k + nconv);
     kc_new = min(kc_new, m - 1);  // pca.pyx:1201-1202
@@ -277,7 +291,6 @@ k_restart_check(const float* __restrict__ Ub, const float* __restrict__ Sb,
     st->k_current = (int)kc_new;
     st->remainder_norm = (float)rn;
     st->smax = S;
-    rn_s = rn;
     conv_s = conv;
     kc_s = (int)kc_new;
   }

@@ -75,9 +75,39 @@ __global__ void k_build_tail(const double* __restrict__ B, uint32_t m, uint32_t 
   }
 }
 
-// Poles, sorted ascending, and deflation. One block; the sequential scan
-// works on shared-memory copies (a global round trip per step would cost
-// more than the rest of the merge).
+// Tails of one or two rows in closed form. The tail's last column is B's
+// column m, which stays zero (pca.pyx:1129-1162): t = 1 gives L = [0]; t = 2
+// gives L = [[beta, 0], [alpha, 0]], so L L^T = v v^T with v = (beta, alpha).
+__global__ void k_tail_small(const double* __restrict__ B, uint32_t m, uint32_t kc,
+                             double* __restrict__ Q, double* __restrict__ sig) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t t = m - kc;
+  if (t == 1) {
+    Q[0] = 1.0;
+    sig[0] = 0.0;
+    return;
+  }
+  const double beta = B[kc + (uint64_t)(kc + 1) * m];
+  const double alpha = B[(kc + 1) + (uint64_t)(kc + 1) * m];
+  const double r = hypot(beta, alpha);
+  if (r > 0.0) {
+    Q[0] = beta / r;   // column 0: v / |v|
+    Q[1] = alpha / r;
+    Q[2] = -alpha / r; // column 1: v rotated a quarter turn
+    Q[3] = beta / r;
+  } else {
+    Q[0] = 1.0; Q[1] = 0.0; Q[2] = 0.0; Q[3] = 1.0;
+  }
+  sig[0] = r;
+  sig[1] = 0.0;
+}
+
+// Poles, sorted ascending, and deflation. One block, in parallel: GB300's
+// FP64 latency makes a thread walking the poles one by one the slowest part
+// of the merge, so the sums, the single-component test, the close-pole test
+// (against each pole's previous surviving pole) and the compaction run
+// across the block. Only when some close pair needs a rotation (rare) does
+// one thread redo the scan sequentially, as rotations can chain.
 __global__ void __launch_bounds__(256)
 k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
               const double* __restrict__ Q, const double* __restrict__ sig_t,
@@ -89,9 +119,13 @@ k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
   double* zs = ds + m;
   int* src = reinterpret_cast<int*>(zs + m);
   int* defl = src + m;
+  __shared__ double red[2][8];
+  __shared__ double tol_s, znrm_s;
+  __shared__ int any_rot, cnt_w[2][8];
   const uint32_t t = m - kc;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const double alpha = B[kc + (uint64_t)kc * m];
-  for (uint32_t l = threadIdx.x; l < m; l += blockDim.x) {
+  for (uint32_t l = tid; l < m; l += blockDim.x) {
     if (l < kc) {
       const double sv = B[l + (uint64_t)l * m];
       d0[l] = sv * sv;
@@ -102,8 +136,9 @@ k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
       z0[l] = alpha * Q[(uint64_t)j * t];  // row 0 of Q, column j
     }
   }
+  if (tid == 0) any_rot = 0;
   __syncthreads();
-  for (uint32_t l = threadIdx.x; l < m; l += blockDim.x) {  // rank sort
+  for (uint32_t l = tid; l < m; l += blockDim.x) {  // rank sort
     const double dl = d0[l];
     uint32_t rank = 0;
     for (uint32_t q = 0; q < m; ++q) {
@@ -115,63 +150,127 @@ k_merge_setup(const double* __restrict__ B, uint32_t m, uint32_t kc,
     src[rank] = (int)l;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // one sequential O(m) scan: tolerance, then single-component and
-    // close-pole deflation in ascending order
-    double zn2 = 0.0, dmax = 0.0;
-    for (uint32_t l = 0; l < m; ++l) {
-      zn2 += zs[l] * zs[l];
-      dmax = fmax(dmax, fabs(ds[l]));
+  // |z|^2 and max |d|: per-thread runs, a fixed shuffle tree, warps in order
+  {
+    double a = 0.0, b = 0.0;
+    for (uint32_t l = tid; l < m; l += blockDim.x) {
+      a += zs[l] * zs[l];
+      b = fmax(b, fabs(ds[l]));
     }
-    const double znrm = sqrt(zn2);
-    const double tol = 8.0 * kEps * fmax(dmax, zn2);
-    int nrot = 0, nnd = 0, ndef = 0;
-    int prev = -1;
-    for (uint32_t l = 0; l < m; ++l) {
-      if (fabs(zs[l]) * znrm <= tol) {
-        defl[l] = 1;
-        continue;
-      }
-      defl[l] = 0;
-      if (prev >= 0) {
-        const double zp = zs[prev], zq = zs[l];
-        const double r = hypot(zp, zq);
-        const double c = zq / r, sn = zp / r;
-        if (fabs((ds[l] - ds[prev]) * c * sn) <= tol) {
-          const double dp = ds[prev], dq = ds[l];
-          ds[prev] = dp * c * c + dq * sn * sn;
-          ds[l] = dp * sn * sn + dq * c * c;
-          zs[prev] = 0.0;
-          zs[l] = r;
-          defl[prev] = 1;
-          w.rot_p[nrot] = prev;
-          w.rot_q[nrot] = (int)l;
-          w.rot_c[nrot] = c;
-          w.rot_s[nrot] = sn;
-          ++nrot;
-        }
-      }
-      prev = (int)l;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
     }
-    double zz = 0.0;
-    for (uint32_t l = 0; l < m; ++l) {
-      if (defl[l]) {
-        w.defpos[ndef++] = (int)l;
-      } else {
-        w.ndpos[nnd] = (int)l;
-        w.dn[nnd] = ds[l];
-        w.zn[nnd] = zs[l];
-        zz += zs[l] * zs[l];
-        ++nnd;
+    if (lane == 0) { red[0][wid] = a; red[1][wid] = b; }
+    __syncthreads();
+    if (tid == 0) {
+      double zn2 = 0.0, dmax = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+        zn2 += red[0][q];
+        dmax = fmax(dmax, red[1][q]);
       }
+      znrm_s = sqrt(zn2);
+      tol_s = 8.0 * kEps * fmax(dmax, zn2);
     }
-    w.state[0] = nnd;
-    w.state[1] = nrot;
-    w.state[2] = ndef;
-    w.znorm2[0] = zz;
+    __syncthreads();
+  }
+  const double tol = tol_s, znrm = znrm_s;
+  for (uint32_t l = tid; l < m; l += blockDim.x) defl[l] = fabs(zs[l]) * znrm <= tol;
+  __syncthreads();
+  for (uint32_t l = tid; l < m; l += blockDim.x) {  // close poles
+    if (defl[l]) continue;
+    int p = (int)l - 1;
+    while (p >= 0 && defl[p]) --p;
+    if (p < 0) continue;
+    const double zp = zs[p], zq = zs[l];
+    const double r = hypot(zp, zq);
+    if (fabs((ds[l] - ds[p]) * (zq / r) * (zp / r)) <= tol) any_rot = 1;
   }
   __syncthreads();
-  for (uint32_t l = threadIdx.x; l < m; l += blockDim.x) {  // for the later kernels
+  int nrot = 0;
+  if (any_rot) {
+    if (tid == 0) {  // the sequential scan: rotations can chain
+      int prev = -1;
+      for (uint32_t l = 0; l < m; ++l) {
+        if (defl[l]) continue;
+        if (prev >= 0) {
+          const double zp = zs[prev], zq = zs[l];
+          const double r = hypot(zp, zq);
+          const double c = zq / r, sn = zp / r;
+          if (fabs((ds[l] - ds[prev]) * c * sn) <= tol) {
+            const double dp = ds[prev], dq = ds[l];
+            ds[prev] = dp * c * c + dq * sn * sn;
+            ds[l] = dp * sn * sn + dq * c * c;
+            zs[prev] = 0.0;
+            zs[l] = r;
+            defl[prev] = 1;
+            w.rot_p[nrot] = prev;
+            w.rot_q[nrot] = (int)l;
+            w.rot_c[nrot] = c;
+            w.rot_s[nrot] = sn;
+            ++nrot;
+          }
+        }
+        prev = (int)l;
+      }
+      cnt_w[0][0] = nrot;
+    }
+    __syncthreads();
+    nrot = cnt_w[0][0];
+    __syncthreads();
+  }
+  // compaction in ascending order: per-thread contiguous runs, then offsets
+  {
+    const uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = min(m, tid * per), b2 = min(m, a + per);
+    int cd = 0;
+    for (uint32_t l = a; l < b2; ++l) cd += defl[l];
+    const int cn = (int)(b2 - a) - cd;
+    int incl_d = cd, incl_n = cn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int vd = __shfl_up_sync(0xffffffffu, incl_d, o);
+      const int vn = __shfl_up_sync(0xffffffffu, incl_n, o);
+      if (lane >= o) { incl_d += vd; incl_n += vn; }
+    }
+    if (lane == 31) { cnt_w[0][wid] = incl_d; cnt_w[1][wid] = incl_n; }
+    __syncthreads();
+    int off_d = 0, off_n = 0;
+    for (int q = 0; q < wid; ++q) { off_d += cnt_w[0][q]; off_n += cnt_w[1][q]; }
+    int pd = off_d + incl_d - cd, pn = off_n + incl_n - cn;
+    for (uint32_t l = a; l < b2; ++l) {
+      if (defl[l]) {
+        w.defpos[pd++] = (int)l;
+      } else {
+        w.ndpos[pn] = (int)l;
+        w.dn[pn] = ds[l];
+        w.zn[pn] = zs[l];
+        ++pn;
+      }
+    }
+    if (tid == (int)blockDim.x - 1) {
+      w.state[0] = pn;
+      w.state[1] = nrot;
+      w.state[2] = pd;
+    }
+  }
+  __syncthreads();
+  {  // |z|^2 over the surviving poles (the last root's bracket)
+    double a = 0.0;
+    for (uint32_t l = tid; l < m; l += blockDim.x)
+      if (!defl[l]) a += zs[l] * zs[l];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[0][wid] = a;
+    __syncthreads();
+    if (tid == 0) {
+      double zz = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) zz += red[0][q];
+      w.znorm2[0] = zz;
+    }
+  }
+  for (uint32_t l = tid; l < m; l += blockDim.x) {  // for the later kernels
     w.ds[l] = ds[l];
     w.src[l] = src[l];
   }
@@ -292,18 +391,20 @@ k_merge_zhat(MergeWork w) {
 // descending order (ties by id). One block.
 __global__ void __launch_bounds__(256)
 k_merge_order(uint32_t m, MergeWork w) {
+  extern __shared__ double lam[];
   const int n = w.state[0];
   for (uint32_t id = threadIdx.x; id < m; id += blockDim.x)
-    w.lam[id] = (int)id < n ? w.dn[w.korig[id]] + w.tau[id] : w.ds[w.defpos[id - n]];
+    lam[id] = (int)id < n ? w.dn[w.korig[id]] + w.tau[id] : w.ds[w.defpos[id - n]];
   __syncthreads();
   for (uint32_t id = threadIdx.x; id < m; id += blockDim.x) {
-    const double li = w.lam[id];
+    const double li = lam[id];
     uint32_t rank = 0;
     for (uint32_t q = 0; q < m; ++q) {
-      const double lq = w.lam[q];
+      const double lq = lam[q];
       rank += (lq > li || (lq == li && q < id)) ? 1u : 0u;
     }
     w.order[rank] = (int)id;
+    w.lam[id] = li;
   }
 }
 
@@ -457,17 +558,23 @@ int launch_svd_merge(const double* B, uint32_t m, uint32_t kc, float* Ub, float*
   // 1. the tail's SVD: FP64 Jacobi for a few rows, else the general FP32
   //    Jacobi + FP64 Newton refinement at size t
   const bool small = t <= kMergeFp64TailMax;
-  k_build_tail<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(tt1, 256), 1024)),
-                 256, 0, s>>>(B, m, kc, L64, small ? nullptr : L32);
-  BGPU_CHECK_LAUNCH();
-  if (small) {
-    BGPU_TRY(launch_jacobi_svd(nullptr, L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t,
-                               jacobi_gwork, nullptr, s, Q64));
+  if (t <= 2) {
+    k_tail_small<<<1, 32, 0, s>>>(B, m, kc, Q64, sb_t);
+    BGPU_CHECK_LAUNCH();
   } else {
-    BGPU_TRY(launch_jacobi_svd(L32, nullptr, t, Ub_t, Sb_t, Vbt_t, nullptr, nullptr,
-                               jacobi_gwork, nullptr, s));
-    BGPU_TRY(launch_svd_refine(L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t, refine_work,
-                               refine_steps, s, Q64));
+    const unsigned tb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(tt1, 256),
+                                                                          1024));
+    k_build_tail<<<tb, 256, 0, s>>>(B, m, kc, L64, small ? nullptr : L32);
+    BGPU_CHECK_LAUNCH();
+    if (small) {
+      BGPU_TRY(launch_jacobi_svd(nullptr, L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t,
+                                 jacobi_gwork, nullptr, s, Q64));
+    } else {
+      BGPU_TRY(launch_jacobi_svd(L32, nullptr, t, Ub_t, Sb_t, Vbt_t, nullptr, nullptr,
+                                 jacobi_gwork, nullptr, s));
+      BGPU_TRY(launch_svd_refine(L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t, refine_work,
+                                 refine_steps, s, Q64));
+    }
   }
   // 2. the merge
   k_merge_setup<<<1, 256, (size_t)4 * m * 8 + (size_t)2 * m * 4, s>>>(B, m, kc, Q64,
@@ -477,7 +584,7 @@ int launch_svd_merge(const double* B, uint32_t m, uint32_t kc, float* Ub, float*
   BGPU_CHECK_LAUNCH();
   k_merge_zhat<<<m, 32, 0, s>>>(w);
   BGPU_CHECK_LAUNCH();
-  k_merge_order<<<1, 256, 0, s>>>(m, w);
+  k_merge_order<<<1, 256, (size_t)m * 8, s>>>(m, w);
   BGPU_CHECK_LAUNCH();
   const size_t vsm = (size_t)3 * m * 8;
   if (vsm > 48 * 1024)
