@@ -7,7 +7,8 @@ Two stages, both writing only under ``oracle/_ref/`` (git-ignored):
 1. ``cythonize`` (needs Cython and the reference checkout): translate the
    reference modules on the path -- ``brisc/cyutils.pyx``, ``brisc/pca.pyx``,
    ``brisc/normalize.pyx``, ``brisc/cysparse.pyx``, ``brisc/hvg.pyx``,
-   ``brisc/kmeans.pyx``, ``brisc/knn.pyx`` -- plus the test harness
+   ``brisc/kmeans.pyx``, ``brisc/knn.pyx``, ``brisc/harmonize.pyx`` -- plus
+   the test harness
    ``oracle/ref_probe.pyx`` to C++ under ``oracle/_ref/gen/``. The sources are
    read where they lie; nothing is copied into the repository.
 2. ``compile`` (needs only g++, Python and numpy headers): build every
@@ -42,11 +43,12 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 GEN = REF_OUT / "gen"
-MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn"]
+MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn",
+           "harmonize"]
 # What the CPU baselines need (cysparse's 24 MB of C++ is only needed for the
 # transpose fixture and is skipped where compile time matters).
 BASELINE_MODULES = ["cyutils", "pca", "normalize", "hvg", "kmeans", "knn",
-                    "ref_probe"]
+                    "harmonize", "ref_probe"]
 DIRECTIVES = {"language_level": "3", "boundscheck": False,
               "wraparound": False, "cdivision": True,
               "initializedcheck": False, "warn.undeclared": False}

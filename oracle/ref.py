@@ -58,11 +58,11 @@ def load(build: bool = True):
         sys.path.insert(0, str(d))
     _mods = {}
     for name in ("cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn",
-                 "ref_probe"):
+                 "harmonize", "ref_probe"):
         try:
             _mods[name] = importlib.import_module(f"brisc.{name}")
         except ImportError:
-            if name not in ("cysparse", "hvg", "kmeans", "knn"):
+            if name not in ("cysparse", "hvg", "kmeans", "knn", "harmonize"):
                 raise
     return _mods
 
@@ -259,3 +259,49 @@ def run_knn_self(prep: dict, num_threads: int | None = None):
             chunk_size_search=prep["chunk_size_search"], is_mac=False,
             num_threads=num_threads or os.cpu_count() or 1)
     return neighbors, distances, near, cdist
+
+
+def run_harmonize(PCs, batch_labels, num_batches: int, num_clusters=None,
+                  max_iterations: int = 10, num_kmeans_iterations: int = 25,
+                  kmeans_tolerance: float = 1e-2, max_clustering_iterations: int = 5,
+                  block_proportion: float = 0.05, tolerance: float = 0.01,
+                  early_stopping: bool = False, clustering_tolerance: float = 1e-3,
+                  theta: float = 2, tau: float = 0, alpha: float = 0.2,
+                  sigma: float = 0.1, chunk_size_kmeans=None, chunk_size_Harmony=None,
+                  seed: int = 0, num_threads: int | None = None) -> dict:
+    """The reference's harmonize() core for one dataset (every cell passing
+    QC): row-normalised PCs (brisc/harmonize.pyx:244 normalize_rows), its
+    kmeans on them for the initial centroids, and harmony
+    (brisc/harmonize.pyx:269), with the argument preparation of
+    brisc/single_cell.py:13777-13876. Returns Z (the Harmony embedding), R,
+    the initial Y and the k-means iteration count."""
+    M = load()
+    H = M["harmonize"]
+    PCs = np.ascontiguousarray(PCs, dtype=np.float32)
+    n, d = PCs.shape
+    num_threads = num_threads or os.cpu_count() or 1
+    if num_clusters is None:
+        num_clusters = max(min(100, int(round(n / 30))), 1)
+    chunk_size_kmeans = chunk_size_kmeans or min(4096, n)
+    chunk_size_Harmony = chunk_size_Harmony or min(256, n)
+    Z = np.empty((n, d), dtype=np.float32)
+    H.normalize_rows(arr=PCs, out=Z, num_threads=num_threads)
+    km = run_kmeans(Z, num_clusters, num_kmeans_iterations=num_kmeans_iterations,
+                    kmeans_tolerance=kmeans_tolerance, chunk_size=chunk_size_kmeans,
+                    seed=seed, num_threads=num_threads)
+    Y0 = km["centroids_new"] if km["iterations"] & 1 else km["centroids"]
+    Y = np.ascontiguousarray(Y0[:num_clusters]).copy()
+    Y_init = Y.copy()
+    R = np.empty((n, num_clusters), dtype=np.float32)
+    with _blas1():
+        H.harmony(PCs=PCs, Z=Z, Y=Y, R=R,
+                  batch_labels=np.ascontiguousarray(batch_labels, dtype=np.uint32),
+                  num_batches=num_batches, max_iterations=max_iterations,
+                  max_clustering_iterations=max_clustering_iterations,
+                  block_proportion=block_proportion, tolerance=tolerance,
+                  early_stopping=early_stopping, clustering_tolerance=clustering_tolerance,
+                  theta=theta, tau=tau, alpha=alpha, sigma=sigma,
+                  chunk_size=chunk_size_Harmony, seed=seed, verbose=False,
+                  num_threads=num_threads)
+    return dict(Z=Z, R=R, Y_init=Y_init, Y=Y, kmeans_iterations=km["iterations"],
+                num_clusters=num_clusters)
