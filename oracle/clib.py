@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
             "oracle_normalize_csr": (None, [vp, vp, u64, vp, i, vp, vp, vp, vp]),
             "oracle_clipped_stddev_csc": (None, [vp, vp, u64, u32, f, vp]),
             "oracle_thread_offsets": (None, [vp, u64, u32, vp]),
+            "oracle_fisher_yates": (None, [u64, u32, vp]),
+            "oracle_kmeans_init": (None, [u64, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -118,3 +120,17 @@ def thread_offsets(indptr, num_threads: int) -> np.ndarray:
     out = np.empty(num_threads + 1, dtype=np.uint32)
     lib().oracle_thread_offsets(_p(ip), ip.shape[0] - 1, num_threads, _p(out))
     return out
+
+
+def fisher_yates(n: int, seed: int) -> np.ndarray:
+    """brisc/harmonize.pyx:503-509's random cell order."""
+    out = np.zeros(n, dtype=np.uint32)
+    lib().oracle_fisher_yates(seed & 0xFFFFFFFFFFFFFFFF, n, _p(out))
+    return out.astype(np.int64)
+
+
+def kmeans_init(n: int, num_clusters: int, seed: int) -> np.ndarray:
+    """brisc/kmeans.pyx:13-38's random initial cells."""
+    out = np.zeros(num_clusters, dtype=np.uint32)
+    lib().oracle_kmeans_init(seed & 0xFFFFFFFFFFFFFFFF, n, num_clusters, _p(out))
+    return out.astype(np.int64)

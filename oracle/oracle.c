@@ -183,3 +183,47 @@ void oracle_thread_offsets(const int64_t* indptr, uint64_t num_major,
   }
   offsets[num_threads] = (uint32_t)num_major;
 }
+
+/* Lemire's bounded integer (brisc/cyutils.pyx:1161-1172). */
+static uint32_t oracle_randint(uint32_t bound, uint64_t* state) {
+  uint64_t m = (uint64_t)oracle_rand(state) * (uint64_t)bound;
+  uint32_t l = (uint32_t)m;
+  if (l < bound) {
+    uint32_t threshold = (0u - bound) % bound;
+    while (l < threshold) {
+      m = (uint64_t)oracle_rand(state) * (uint64_t)bound;
+      l = (uint32_t)m;
+    }
+  }
+  return (uint32_t)(m >> 32);
+}
+
+/* The "inside-out" Fisher-Yates cell order of brisc/harmonize.pyx:503-509,
+ * from srand(seed). */
+void oracle_fisher_yates(uint64_t seed, uint32_t n, uint32_t* order) {
+  uint64_t state = oracle_srand(seed);
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t j = oracle_randint(i + 1, &state);
+    order[i] = order[j];
+    order[j] = i;
+  }
+}
+
+/* The random k-means initialisation of brisc/kmeans.pyx:13-38: num_clusters
+ * distinct cells drawn from srand(seed). */
+void oracle_kmeans_init(uint64_t seed, uint32_t n, uint32_t nc, uint32_t* cells) {
+  uint64_t state = oracle_srand(seed);
+  uint64_t words = ((uint64_t)n + 63) / 64;
+  uint64_t* bits = (uint64_t*)calloc(words, 8);
+  for (uint32_t i = 0; i < nc; ++i) {
+    for (;;) {
+      uint32_t j = oracle_randint(n, &state);
+      if (!(bits[j >> 6] & (1ull << (j & 63)))) {
+        bits[j >> 6] |= 1ull << (j & 63);
+        cells[i] = j;
+        break;
+      }
+    }
+  }
+  free(bits);
+}
