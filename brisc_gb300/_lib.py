@@ -137,6 +137,9 @@ SIGNATURES = {
                            _u32, _u32, _u32, _vp]),
     "bgpu_kmeans": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _u32, _f, _u32, _u64,
                          _u64, _u32, _u32, C.POINTER(_u32), _vp]),
+    "bgpu_normalize_rows": (_i, [_vp, _vp, _u64, _u32, _vp]),
+    "bgpu_harmony": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f, _f, _i, _f, _f,
+                          _f, _f, _f, _u32, _u64, _u64, _u32, _u32, C.POINTER(_u32), _vp]),
 }
 
 _lock = threading.Lock()

@@ -400,6 +400,34 @@ BGPU_API int bgpu_kmeans(const float* X, uint32_t* cluster_labels, float* centro
                          uint32_t num_dimensions, uint32_t num_clusters,
                          uint32_t* iterations, void* stream);
 
+/* normalize_rows (brisc/harmonize.pyx:244-266, called by
+ * SingleCell.harmonize at brisc/single_cell.py:13819): out = arr with each
+ * row scaled to unit Euclidean norm. num_rows x num_columns row-major
+ * float32, device pointers; arr == out is allowed. Asynchronous on stream. */
+BGPU_API int bgpu_normalize_rows(const float* arr, float* out, uint64_t num_rows,
+                                 uint32_t num_columns, void* stream);
+
+/* harmony (brisc/harmonize.pyx:269-871, called by SingleCell.harmonize at
+ * brisc/single_cell.py:13864-13875). Same arguments as the reference, minus
+ * verbose and num_threads: PCs (num_cells x num_PCs), Z (the row-normalised
+ * PCs on entry, the Harmony embedding on return), Y (num_clusters x num_PCs:
+ * the k-means centroids of Z on entry, the last normalised centroids on
+ * return), R (num_cells x num_clusters soft assignments, output),
+ * batch_labels (uint32 per cell, < num_batches). The cells are visited in the
+ * reference's PCG32 Fisher-Yates order from seed, in blocks of
+ * ceil(num_cells * block_proportion) cells and chunks of chunk_size cells
+ * within a block. *iterations receives the number of correction rounds run.
+ * Device pointers; synchronous. Limits: num_PCs <= 128, num_clusters <= 256,
+ * num_batches <= 64, chunk_size <= 1024, num_cells < 2^32. */
+BGPU_API int bgpu_harmony(const float* PCs, float* Z, float* Y, float* R,
+                          const uint32_t* batch_labels, uint32_t num_batches,
+                          uint32_t max_iterations, uint32_t max_clustering_iterations,
+                          float block_proportion, float tolerance, int early_stopping,
+                          float clustering_tolerance, float theta, float tau, float alpha,
+                          float sigma, uint32_t chunk_size, uint64_t seed,
+                          uint64_t num_cells, uint32_t num_PCs, uint32_t num_clusters,
+                          uint32_t* iterations, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,8 +64,12 @@ def harmony(PCs, Z, Y, batch, num_batches: int, max_iterations: int = 10,
     N_b = np.bincount(batch, minlength=B).astype(np.int64)
     Pr_b = (N_b.astype(F) / F(n)).astype(F)
     if tau > 0:
-        base = np.exp(-N_b / (C * tau)).astype(F)
-        theta_b = (F(theta) * (F(1) - base * base)).astype(F)
+        # harmonize.pyx:416 negates an unsigned count: -N_b wraps to
+        # 2^32 - N_b, so base is inf (1 for an empty batch) and theta -inf
+        neg = (np.uint32(0) - N_b.astype(np.uint32)).astype(F)
+        with np.errstate(over="ignore"):
+            base = np.exp((neg / (F(C) * F(tau))).astype(np.float64)).astype(F)
+            theta_b = (F(theta) * (F(1) - base * base)).astype(F)
     else:
         theta_b = np.full(B, theta, dtype=F)
     tos = F(2) / F(sigma)
@@ -79,7 +83,8 @@ def harmony(PCs, Z, Y, batch, num_batches: int, max_iterations: int = 10,
     prev = _objective(Z, Y, R, O, E, theta_b, sigma)
     Y = normalize_rows(Y)
     order = _pcg_order(n, seed)
-    block = int(np.ceil(n * block_proportion))
+    # an unsigned long long times a float in the reference: a float product
+    block = int(np.ceil(F(n) * F(block_proportion)))
     objective = prev
     for _ in range(max_iterations):
         past = []

@@ -182,3 +182,16 @@ def pca_like(num_cells: int, num_dims: int, components: int, seed: int) -> np.nd
     lab = rng.integers(0, components, num_cells)
     X = centres[lab] + 0.35 * rng.standard_normal((num_cells, num_dims)) * scale
     return np.ascontiguousarray(X.astype(np.float32))
+
+
+def batched_pcs(num_cells: int, num_dims: int, components: int, num_batches: int,
+                seed: int, shift: float = 2.0):
+    """Seeded stand-in for the PCs of several batches: ``pca_like`` cells,
+    each given a uniformly drawn batch label and its batch's offset (a
+    ``shift``-scaled Gaussian vector per batch) -- the batch effect Harmony
+    removes. Returns (PCs float32, batch labels uint32)."""
+    X = pca_like(num_cells, num_dims, components, seed)
+    rng = np.random.default_rng((seed, 1))
+    labels = rng.integers(0, num_batches, num_cells).astype(np.uint32)
+    offsets = (rng.standard_normal((num_batches, num_dims)) * shift).astype(np.float32)
+    return np.ascontiguousarray((X + offsets[labels]).astype(np.float32)), labels

@@ -25,6 +25,15 @@ reference's outputs, so the tests never regenerate data:
                  Gaussian-mixture "PCs" (regenerated from the seed, with a
                  fingerprint): the k-means outputs knn_self takes and its
                  neighbours, distances and nearest clusters.
+* harmony.npz    the reference's harmonize() core (brisc/single_cell.py:
+                 13776-13875: normalize_rows, kmeans, harmony at
+                 brisc/harmonize.pyx:269) on seeded batch-shifted "PCs"
+                 (synth.batched_pcs, regenerated from the seed, with a
+                 fingerprint): the k-means centroids harmony starts from, the
+                 embedding Z, the first rows of R and the k-means iteration
+                 count, for the default settings, for one case with early
+                 stopping, a larger block and a smaller chunk, and for
+                 tau > 0 (where the reference's output is NaN).
 * hvg.npz        gene_mean_and_variance_csr/_csc and clipped_sum_csr/_csc
                  (brisc/hvg.pyx) on an NB count matrix with a few large
                  counts, over all cells and over a cell subset, uint32 and
@@ -34,6 +43,7 @@ reference's outputs, so the tests never regenerate data:
     python tests/golden/make_golden.py hvg      # hvg.npz only
     python tests/golden/make_golden.py parity   # parity50k.npz only
     python tests/golden/make_golden.py knn      # knn.npz only
+    python tests/golden/make_golden.py harmony  # harmony.npz only
 """
 from __future__ import annotations
 
@@ -163,6 +173,39 @@ def make_knn() -> None:
     np.savez_compressed(OUT / "knn.npz", **out)
 
 
+HARMONY_CASES = {  # name: (cells, dims, components, batches, seed, harmony keywords)
+    "harm_a": (3000, 20, 12, 3, 9, {}),
+    "harm_b": (2500, 30, 8, 4, 11, dict(num_clusters=40, early_stopping=True,
+                                         block_proportion=0.1, chunk_size_Harmony=100,
+                                         max_clustering_iterations=6, seed=3)),
+    # tau > 0: the reference's discount negates an unsigned count, so its
+    # theta is -inf and its output NaN (harmonize.pyx:416)
+    "harm_tau": (800, 10, 5, 2, 13, dict(tau=5.0, max_iterations=2)),
+}
+HARMONY_R_ROWS = 400  # rows of R stored
+
+
+def make_harmony() -> None:
+    import hashlib
+    import json
+    from synth import batched_pcs
+    out = {}
+    for name, (n, d, comps, B, seed, kw) in HARMONY_CASES.items():
+        X, labels = batched_pcs(n, d, comps, B, seed)
+        r = ref.run_harmonize(X, labels, B, num_threads=1, **kw)
+        out[f"{name}_shape"] = np.array([n, d, comps, B, seed])
+        out[f"{name}_kwargs"] = np.array(json.dumps(kw))
+        out[f"{name}_fingerprint"] = np.array(
+            hashlib.sha256(X.tobytes() + labels.tobytes()).hexdigest())
+        out[f"{name}_Y_init"] = r["Y_init"]
+        out[f"{name}_Z"] = r["Z"]
+        out[f"{name}_R_head"] = r["R"][:HARMONY_R_ROWS]
+        out[f"{name}_kmeans_iterations"] = np.array(r["kmeans_iterations"])
+        print(name, "clusters", r["num_clusters"], "k-means iterations",
+              r["kmeans_iterations"])
+    np.savez_compressed(OUT / "harmony.npz", **out)
+
+
 def main() -> int:
     M = ref.load()
     if M is None:
@@ -174,10 +217,15 @@ def main() -> int:
     if sys.argv[1:] == ["knn"]:
         make_knn()
         return 0
+    if sys.argv[1:] == ["harmony"]:
+        make_harmony()
+        return 0
     if "hvg" in M:
         make_hvg(M)
     if "knn" in M and not sys.argv[1:]:
         make_knn()
+    if "harmonize" in M and not sys.argv[1:]:
+        make_harmony()
     if sys.argv[1:] == ["hvg"]:
         return 0
     probe = M["ref_probe"]

@@ -139,3 +139,26 @@ def test_knn_self_argument_checks_before_any_device_work():
         knn.knn_self(**bad)
     with _pt.raises(ValueError, match="chunk_size_search"):
         knn.knn_self(**good, chunk_size_search=0)
+
+
+def test_harmony_argument_checks_before_any_device_work(built_lib):
+    """bgpu_harmony rejects NULL pointers and sizes beyond its limits before
+    it touches memory (the pointers below are never dereferenced)."""
+    from brisc_gb300 import _lib
+    L = _lib.lib()
+    it = C.c_uint32(0)
+    p = C.c_void_p(256)
+
+    def run(B=3, d=20, nc=50, chunk=256, n=1000, bp=0.05, sigma=0.1, null=False):
+        ptrs = [None] * 5 if null else [p] * 5
+        return L.bgpu_harmony(*ptrs, B, 10, 5, bp, 0.01, 0, 1e-3, 2.0, 0.0, 0.2, sigma,
+                              chunk, 0, n, d, nc, C.byref(it), None)
+    assert run(null=True) == _lib.ERR_INVALID
+    assert run(B=65) == _lib.ERR_UNSUPPORTED
+    assert run(d=129) == _lib.ERR_UNSUPPORTED
+    assert run(nc=257) == _lib.ERR_UNSUPPORTED
+    assert run(chunk=2000) == _lib.ERR_UNSUPPORTED
+    assert run(bp=0.0) == _lib.ERR_INVALID
+    assert run(sigma=0.0) == _lib.ERR_INVALID
+    assert b"sigma" in L.bgpu_last_error()
+    assert L.bgpu_normalize_rows(None, None, 5, 3, None) == _lib.ERR_INVALID

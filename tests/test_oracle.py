@@ -201,3 +201,43 @@ def test_knn_oracle_matches_reference(golden, name):
         c["X"], c["sorted_order"], c["centroids"], c["num_cells_per_cluster"],
         c["cell_norms"], c["num_neighbors"], c["num_clusters_searched"])
     check_against(c, nbr, dist, near, cdist)
+
+
+@pytest.mark.parametrize("name", ["harm_a", "harm_b"])
+def test_harmony_oracle_matches_reference(golden, name):
+    """oracle/harmony.py (the NumPy restatement of brisc/harmonize.pyx:269)
+    against the compiled reference's harmony from the same k-means centroids:
+    the embedding within 3e-6 of max |Z| (float rounding amplified by the
+    iterations; 6e-7 measured), every row's direction within 1e-9 of cosine
+    1, the first 400 rows of R within 2e-5. Agreement at this level also
+    pins the PCG32 Fisher-Yates cell order the restatement draws."""
+    from harmony_cases import case, check_against
+    from oracle import harmony as oh
+    c = case(golden("harmony"), name)
+    Z, R = oh.harmony(c["PCs"], oh.normalize_rows(c["PCs"]), c["Y_init"],
+                      c["batch_labels"], c["num_batches"], **c["harmony_kwargs"])
+    check_against(c, Z, R[:len(c["ref_R_head"])], z_rel=3e-6, r_abs=2e-5,
+                  min_cos=1 - 1e-9)
+
+
+def test_harmony_oracle_tau_matches_reference_nan(golden):
+    """With tau > 0 the reference's theta discount negates an unsigned count
+    (brisc/harmonize.pyx:416) and its output is NaN throughout; the
+    restatement does the same arithmetic."""
+    from harmony_cases import case
+    from oracle import harmony as oh
+    c = case(golden("harmony"), "harm_tau")
+    assert np.isnan(c["ref_Z"]).all() and np.isnan(c["ref_R_head"]).all()
+    with np.errstate(all="ignore"):
+        Z, R = oh.harmony(c["PCs"], oh.normalize_rows(c["PCs"]), c["Y_init"],
+                          c["batch_labels"], c["num_batches"], **c["harmony_kwargs"])
+    assert np.isnan(Z).all() and np.isnan(R).all()
+
+
+def test_fisher_yates_is_a_permutation():
+    """The inside-out Fisher-Yates draw behind Harmony's cell order is a
+    permutation, and a different seed gives a different one."""
+    from oracle import clib
+    a, b = clib.fisher_yates(1000, 0), clib.fisher_yates(1000, 1)
+    assert np.array_equal(np.sort(a), np.arange(1000))
+    assert not np.array_equal(a, b)
