@@ -58,6 +58,8 @@ WORKLOADS = {
     "hvg_1m": (1_000_000, 2000, 0.05, 0, 0),
     # knn_self (brisc/knn.pyx) on 1M cells x 50 PCs, 20 neighbours
     "knn_1m": (1_000_000, 50, 0.0, 20, 0),
+    # harmonize() (brisc/harmonize.pyx) on 1M cells x 50 PCs from 4 batches
+    "harmony_1m": (1_000_000, 50, 0.0, 4, 0),
 }
 # Generator arguments beyond the density: the large solve has 13 cell-type
 # clusters with lognormal(0, 0.8) per-gene mean offsets; their mean factor
@@ -244,6 +246,11 @@ REFERENCE_COUNTS = {"plain_1m": {"restarts": 69, "lanczos_steps": None,
 def run_reference(args):
     ws, rank, _ = dist_init(args)
     if rank != 0:
+        return 0
+    if args.workload in ("hvg_1m", "knn_1m", "harmony_1m"):
+        print(json.dumps({"impl": "reference", "workload": args.workload, "unavailable":
+                          "this workload times the reference's own functions inside its "
+                          "own line (cpu_baseline)"}))
         return 0
     C, k, m = workload(args)
     from oracle import ref
@@ -968,6 +975,135 @@ def run_knn(args):
     return 0
 
 
+def run_harmony(args):
+    """The core of SingleCell.harmonize() (brisc/single_cell.py:13776-13875):
+    normalize_rows, k-means on the normalised PCs, harmony
+    (brisc/harmonize.pyx:269), with the reference's defaults (100 clusters,
+    block_proportion 0.05, chunks of 256, sigma 0.1, theta 2), on 1M cells x
+    50 PCs from 4 batches (seeded Gaussian mixture with a PCA-like spectrum
+    plus a per-batch offset). A step is one harmonize() on device-resident
+    PCs and labels; e2e the same call from host arrays (copies included). The
+    reference's own harmonize core on every host core is the CPU baseline and
+    the parity check (the embeddings compared row by row)."""
+    import torch
+
+    from brisc_gb300 import harmony as H
+    from oracle import ref
+    from synth import batched_pcs
+    torch.cuda.init()
+    dev = torch.device("cuda", 0)
+    n, d, _, B, _ = WORKLOADS[args.workload]
+    if args.cells:
+        n = args.cells
+    X, lab = batched_pcs(n, d, 30, B, seed=0)
+    dX = torch.from_numpy(X).to(dev)
+    dlab = torch.from_numpy(lab.view(np.int32)).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    info = {}
+
+    def step():
+        Z, inf = H.harmonize(dX, dlab, B, return_info=True)
+        info.update(inf)
+        return Z
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            Zd = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / args.steps
+    Zg = Zd.cpu().numpy()
+    # harmony() alone, from the k-means centroids of the last step's pipeline
+    Zn = torch.empty_like(dX)
+    H.normalize_rows(dX, Zn)
+    nc = info["num_clusters"]
+    Y = torch.empty((nc, d), dtype=torch.float32, device=dev)
+    Yn = torch.empty_like(Y)
+    i32 = dict(dtype=torch.int32, device=dev)
+    km_it = H.kmeans(X=Zn, cluster_labels=torch.empty(n, **i32), centroids=Y,
+                     centroids_new=Yn, num_cells_per_cluster=torch.empty(nc, **i32),
+                     min_distances=torch.empty(n, dtype=torch.float32, device=dev),
+                     cell_norms=torch.empty(0, dtype=torch.float32, device=dev),
+                     num_kmeans_iterations=25, tolerance=1e-2, chunk_size=min(4096, n),
+                     seed=0)
+    Y0 = (Yn if km_it & 1 else Y).clone()
+    R = torch.empty((n, nc), dtype=torch.float32, device=dev)
+    h_times = []
+    for _ in range(2):
+        Zh, Yh = Zn.clone(), Y0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h_it = H.harmony(PCs=dX, Z=Zh, Y=Yh, R=R, batch_labels=dlab, num_batches=B)
+        torch.cuda.synchronize()
+        h_times.append(time.perf_counter() - t0)
+    del Zh, Yh, R, Zn
+
+    # e2e: host arrays through the drop-in
+    e2e_steps = args.e2e_steps or min(3, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Zh_host = H.harmonize(X, lab, B)
+    e2e = (time.perf_counter() - t0) / e2e_steps
+    same_paths = bool(np.array_equal(Zh_host, Zg))
+
+    # FLOPs of the distance-shaped products (2 per multiply-add): per
+    # clustering iteration the block passes' Z.Y and R^T Z, per correction
+    # round R^T PCs and the Z update; the initial assignments once
+    it, ci = info["iterations"], 5
+    flops = 2.0 * n * nc * d * (1 + it * (2 * ci + 2))
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    block = int(np.ceil(np.float32(n) * np.float32(0.05)))
+    nblocks = -(-n // block)
+    launches = 1 + (1 + 6 * info["kmeans_iterations"] + 3) + \
+        (2 + it * (ci * (2 + nblocks) + 2))
+    cpu, parity = None, None
+    if not args.no_cpu_baseline and ref.load() is not None and "harmonize" in ref.load():
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        r = ref.run_harmonize(X, lab, B, num_threads=cores)
+        t_ref = time.perf_counter() - t0
+        cpu = {"value": t_ref, "unit": "s/harmonize", "cores": cores, "kind": "reference",
+               "sample": "the reference's normalize_rows + kmeans + harmony on the full "
+                         "1M-cell input, every host core"}
+        Zr = r["Z"].astype(np.float64)
+        Z64 = Zg.astype(np.float64)
+        cos = (Z64 * Zr).sum(1) / (np.linalg.norm(Z64, axis=1) * np.linalg.norm(Zr, axis=1))
+        parity = {"max_abs_diff_over_max_abs": float(np.abs(Z64 - Zr).max() / np.abs(Zr).max()),
+                  "min_row_cosine": float(cos.min()), "mean_row_cosine": float(cos.mean()),
+                  "kmeans_iterations_gpu": info["kmeans_iterations"],
+                  "kmeans_iterations_reference": int(r["kmeans_iterations"])}
+    out = {"metric": "harmonize: s per run (1M cells x 50 PCs, 4 batches)",
+           "value": sec, "unit": "s/harmonize", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "higher_is_better": False, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": f"harmony_1m: {n:,} cells x {d} PCs (Gaussian mixture, "
+                                  f"PCA-like spectrum, {B} batch offsets), {nc} clusters, "
+                                  "the reference's defaults",
+                      "l2": "R (400 MB) and the PCs (200 MB) larger than L2 (no flush)"},
+           "harmony_only_seconds": min(h_times), "iterations": it,
+           "kmeans_iterations": info["kmeans_iterations"],
+           "e2e": {"value": e2e, "unit": "s/harmonize",
+                   "h2d_bytes_per_step": int(X.nbytes + lab.nbytes),
+                   "d2h_bytes_per_step": int(X.nbytes)},
+           "roofline": {"bound": "fp32-simt", "achieved": flops / sec / 1e12,
+                        "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": flops / sec / 1e12 / fp32_peak,
+                        "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz)",
+                        "traffic": None, "flops_per_step": flops,
+                        "note": "the block-sequential cluster updates (one launch per "
+                                "block, 20 per pass) bound the time, not the FLOPs"},
+           "cpu_baseline": cpu, "agreement_with_reference": parity,
+           "host_and_device_paths_identical": same_paths,
+           "clocks": clk.summary(), "gpu_launches": launches * args.steps}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -976,6 +1112,8 @@ def main():
         return run_hvg(args)
     if args.workload == "knn_1m":
         return run_knn(args)
+    if args.workload == "harmony_1m":
+        return run_harmony(args)
     if args.workload == "batched_3m":
         return run_batched(args)
     if args.workload == "serve":

@@ -99,13 +99,15 @@ def harmonize(PCs, batch_labels, num_batches=None, num_clusters=None,
               tolerance: float = 0.01, early_stopping: bool = False,
               clustering_tolerance: float = 1e-3, theta: float = 2, tau: float = 0,
               alpha: float = 0.2, sigma: float = 0.1, chunk_size_Harmony=None,
-              seed: int = 0):
+              seed: int = 0, return_info: bool = False):
     """The core of SingleCell.harmonize() (brisc/single_cell.py:13776-13875)
     for the float32 PCs of the cells passing QC and their uint32 batch labels:
     default cluster count and chunk sizes with the reference's checks, Z =
     normalize_rows(PCs), k-means on Z (random initialisation), harmony.
     NumPy inputs give a NumPy result; CUDA tensors stay on their device.
-    Returns the Harmony embedding (num_cells x num_PCs, float32)."""
+    Returns the Harmony embedding (num_cells x num_PCs, float32); with
+    return_info, also a dict of the k-means and Harmony iteration counts and
+    the cluster count."""
     import torch
     on_dev = _is_cuda(PCs)
     if on_dev:
@@ -151,14 +153,18 @@ def harmonize(PCs, batch_labels, num_batches=None, num_clusters=None,
     if it & 1:
         Y = Y_new
     R = torch.empty((n, num_clusters), **f32)
-    harmony(PCs=P, Z=Z, Y=Y, R=R, batch_labels=b, num_batches=num_batches,
+    h_it = harmony(PCs=P, Z=Z, Y=Y, R=R, batch_labels=b, num_batches=num_batches,
             max_iterations=max_iterations,
             max_clustering_iterations=max_clustering_iterations,
             block_proportion=block_proportion, tolerance=tolerance,
             early_stopping=early_stopping, clustering_tolerance=clustering_tolerance,
             theta=theta, tau=tau, alpha=alpha, sigma=sigma,
             chunk_size=chunk_size_Harmony, seed=seed)
-    return Z if on_dev else Z.cpu().numpy()
+    out = Z if on_dev else Z.cpu().numpy()
+    if return_info:
+        return out, {"kmeans_iterations": it, "iterations": h_it,
+                     "num_clusters": num_clusters}
+    return out
 
 
 NAMES = ("harmony", "normalize_rows")
