@@ -18,6 +18,15 @@
  *   brisc/normalize.pyx:9-268      normalize_csr             -> bgpu_normalize_csr,
  *                                                               bgpu_size_factors
  *   brisc/cysparse.pyx:1179-1295   csr_tocsc                 -> bgpu_csr_tocsc
+ * and, either side of the path (the gene statistics feeding it, the first
+ * consumers of the PCs):
+ *   brisc/hvg.pyx:9-530            gene_mean_and_variance_*,
+ *                                  clipped_sum_*             -> bgpu_gene_mean_var,
+ *                                                               bgpu_clipped_sum
+ *   brisc/kmeans.pyx:889-1433      kmeans                    -> bgpu_kmeans
+ *   brisc/knn.pyx:13-515           knn_self                  -> bgpu_knn_self
+ *   brisc/harmonize.pyx:244-266    normalize_rows            -> bgpu_normalize_rows
+ *   brisc/harmonize.pyx:269-871    harmony                   -> bgpu_harmony
  */
 #ifndef BRISCGPU_H
 #define BRISCGPU_H
@@ -417,8 +426,12 @@ BGPU_API int bgpu_normalize_rows(const float* arr, float* out, uint64_t num_rows
  * reference's PCG32 Fisher-Yates order from seed, in blocks of
  * ceil(num_cells * block_proportion) cells and chunks of chunk_size cells
  * within a block. *iterations receives the number of correction rounds run.
+ * tau > 0 repeats the reference's arithmetic (its theta discount negates an
+ * unsigned count, harmonize.pyx:416), whose output is then NaN.
  * Device pointers; synchronous. Limits: num_PCs <= 128, num_clusters <= 256,
- * num_batches <= 64, chunk_size <= 1024, num_cells < 2^32. */
+ * num_batches <= 64, chunk_size <= 1024, num_cells < 2^32, and num_PCs x
+ * num_clusters plus three num_batches x num_clusters floats within one CTA's
+ * shared memory (BGPU_ERR_UNSUPPORTED otherwise). */
 BGPU_API int bgpu_harmony(const float* PCs, float* Z, float* Y, float* R,
                           const uint32_t* batch_labels, uint32_t num_batches,
                           uint32_t max_iterations, uint32_t max_clustering_iterations,
