@@ -60,6 +60,8 @@ WORKLOADS = {
     "knn_1m": (1_000_000, 50, 0.0, 20, 0),
     # harmonize() (brisc/harmonize.pyx) on 1M cells x 50 PCs from 4 batches
     "harmony_1m": (1_000_000, 50, 0.0, 4, 0),
+    # the 1M x 2000 counts as an .h5ad file, read straight to the device
+    "h5ad_1m": (1_000_000, 2000, 0.05, 0, 0),
 }
 # Generator arguments beyond the density: the large solve has 13 cell-type
 # clusters with lognormal(0, 0.8) per-gene mean offsets; their mean factor
@@ -247,7 +249,7 @@ def run_reference(args):
     ws, rank, _ = dist_init(args)
     if rank != 0:
         return 0
-    if args.workload in ("hvg_1m", "knn_1m", "harmony_1m"):
+    if args.workload in ("hvg_1m", "knn_1m", "harmony_1m", "h5ad_1m"):
         print(json.dumps({"impl": "reference", "workload": args.workload, "unavailable":
                           "this workload times the reference's own functions inside its "
                           "own line (cpu_baseline)"}))
@@ -1104,6 +1106,132 @@ def run_harmony(args):
     return 0
 
 
+def run_h5ad(args):
+    """The 1M x 2000 NB counts written as an .h5ad file (AnnData's CSR group:
+    float32 data, int32 indices, int64 indptr, superblock 0 as h5py writes by
+    default; h5file.py) and read into device memory. A step is one
+    h5ad.read_X: metadata parse, then host threads pread 16 MB pieces into
+    pinned buffers and copy them to the device. The reference's path to the
+    same device arrays is its own reader (brisc/hdf5.pyx:163
+    read_all_datasets, every host core, into NumPy arrays) followed by a copy
+    of those arrays to the device; its host-only time is reported too. The
+    file is in the page cache for both (written, then read once, before
+    timing). Also: the time to a solver-ready DeviceMatrix from the file
+    (read, size factors, layout)."""
+    import tempfile
+
+    import torch
+
+    import h5file
+    from brisc_gb300 import h5ad
+    from oracle import ref
+    from synth import cached_nb_counts
+    torch.cuda.init()
+    dev = torch.device("cuda", 0)
+    n, g, dens, _, _ = WORKLOADS[args.workload]
+    if args.cells:
+        n = args.cells
+    C = cached_nb_counts(n, g, seed=0, density=dens)
+    data = C.data.astype(np.float32)
+    indices = C.indices.astype(np.int32)
+    indptr = C.indptr.astype(np.int64)
+    nbytes = data.nbytes + indices.nbytes + indptr.nbytes
+    tmpdir = tempfile.mkdtemp(prefix="brisc_h5ad_")
+    path = os.path.join(tmpdir, "counts_1m.h5ad")
+    h5file.write_h5ad(path, data, indices, indptr, (n, g))
+    del data
+    cores = os.cpu_count() or 1
+    try:
+        for _ in range(max(args.warmup, 3)):
+            X = h5ad.read_X(path)
+        torch.cuda.synchronize()
+        times = []
+        with Clocks(0) as clk:
+            for _ in range(args.steps):
+                del X
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                X = h5ad.read_X(path)
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t0)
+        sec = float(np.median(times))
+        same = bool(np.array_equal(X["indptr"].cpu().numpy(), indptr) and
+                    np.array_equal(X["indices"].cpu().numpy(), indices) and
+                    np.array_equal(X["data"].cpu().numpy(), C.data.astype(np.float32)))
+        del X
+        # to a solver-ready matrix
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        M = h5ad.device_matrix(path, method="logCP10k")
+        torch.cuda.synchronize()
+        t_matrix = time.perf_counter() - t0
+        M.close()
+        # the host-to-device link: a pinned 1 GB copy, best of 5
+        hb = torch.empty(1 << 30, dtype=torch.uint8).pin_memory()
+        db = torch.empty(1 << 30, dtype=torch.uint8, device=dev)
+        link = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            db.copy_(hb, non_blocking=True)
+            torch.cuda.synchronize()
+            link.append((1 << 30) / (time.perf_counter() - t0) / 1e9)
+        link_gbs = max(link)
+        del hb, db
+        cpu = None
+        if not args.no_cpu_baseline and ref.load() is not None and "hdf5" in ref.load():
+            info = h5ad.inspect(path)
+            dsets = [(info[k]["file_offset"], info[k]["dtype"], info[k]["num_elements"])
+                     for k in ("data", "indices", "indptr")]
+            ref.run_read_all_datasets(path, dsets, cores)  # warm
+            t_host, t_dev = [], []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                arrs = ref.run_read_all_datasets(path, dsets, cores)
+                t1 = time.perf_counter()
+                on_dev = [torch.from_numpy(a).to(dev) for a in arrs]
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
+                t_host.append(t1 - t0)
+                t_dev.append(t2 - t0)
+                del arrs, on_dev
+            cpu = {"value": float(np.median(t_dev)), "unit": "s/read", "cores": cores,
+                   "kind": "reference",
+                   "sample": "the reference's read_all_datasets (brisc/hdf5.pyx, every host "
+                             "core) of the whole file's X into NumPy arrays, then a copy of "
+                             "them to the device (torch .to(cuda))",
+                   "host_only_seconds": float(np.median(t_host))}
+    finally:
+        try:
+            os.remove(path)
+            os.rmdir(tmpdir)
+        except OSError:
+            pass
+    out = {"metric": "h5ad X to device: s per read (1M x 2000 counts, 829 MB)",
+           "value": sec, "unit": "s/read", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "higher_is_better": False, "dtype": "bytes",
+           "data": "synthetic",
+           "config": {"workload": f"h5ad_1m: {n:,} x {g:,} NB counts ({C.nnz:,} entries) as "
+                                  "an .h5ad CSR group (float32 data, int32 indices, int64 "
+                                  "indptr), superblock 0, contiguous datasets",
+                      "page_cache": "warm (the file was written and read before timing)",
+                      "threads": cores, "bytes": int(nbytes)},
+           "achieved_gbs": nbytes / sec / 1e9, "to_device_matrix_seconds": t_matrix,
+           "bit_identical": same,
+           "e2e": {"value": sec, "unit": "s/read", "h2d_bytes_per_step": int(nbytes),
+                   "d2h_bytes_per_step": 0},
+           "roofline": {"bound": "host-to-device link", "achieved": nbytes / sec / 1e9,
+                        "peak": link_gbs, "unit": "GB/s", "frac": nbytes / sec / 1e9 / link_gbs,
+                        "peak_source": "measured here: a pinned 1 GB torch copy, best of 5",
+                        "traffic": None},
+           "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": 0,
+           "gpu_launches_note": "a read is host threads and cudaMemcpyAsync copies, no "
+                                "kernels; device_matrix then runs the size-factor and "
+                                "layout kernels"}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1114,6 +1242,8 @@ def main():
         return run_knn(args)
     if args.workload == "harmony_1m":
         return run_harmony(args)
+    if args.workload == "h5ad_1m":
+        return run_h5ad(args)
     if args.workload == "batched_3m":
         return run_batched(args)
     if args.workload == "serve":

@@ -13,7 +13,8 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libbriscgpu.so"
 
 # status codes (include/briscgpu.h)
-OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_CANCELLED, ERR_DEVICE = range(7)
+(OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_CANCELLED, ERR_DEVICE,
+ ERR_IO) = range(8)
 INDEX_I32, INDEX_I64 = 0, 1
 VALUE_U16, VALUE_U32, VALUE_I32, VALUE_F32 = 0, 1, 2, 3
 VALUE_I64, VALUE_U64, VALUE_F64 = 4, 5, 6  # the HVG statistics only
@@ -105,6 +106,32 @@ class HvgInput(C.Structure):
     ]
 
 
+H5_I32, H5_I64, H5_U32, H5_U64 = 0, 1, 2, 3  # index arrays in an .h5ad file
+
+
+class H5Dataset(C.Structure):
+    _fields_ = [
+        ("file_offset", C.c_uint64),
+        ("num_bytes", C.c_uint64),
+        ("num_elements", C.c_uint64),
+        ("element_size", C.c_uint32),
+        ("type", C.c_int),
+    ]
+
+
+class H5adMatrix(C.Structure):
+    _fields_ = [
+        ("X_key", C.c_char * 64),
+        ("is_csr", C.c_int),
+        ("num_rows", C.c_uint64),
+        ("num_columns", C.c_uint64),
+        ("nnz", C.c_uint64),
+        ("data", H5Dataset),
+        ("indices", H5Dataset),
+        ("indptr", H5Dataset),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/briscgpu.h declares
 _vp, _u32, _u64, _i, _f = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
 SIGNATURES = {
@@ -140,6 +167,8 @@ SIGNATURES = {
     "bgpu_normalize_rows": (_i, [_vp, _vp, _u64, _u32, _vp]),
     "bgpu_harmony": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f, _f, _i, _f, _f,
                           _f, _f, _f, _u32, _u64, _u64, _u32, _u32, C.POINTER(_u32), _vp]),
+    "bgpu_h5ad_inspect": (_i, [C.c_char_p, C.c_char_p, C.POINTER(H5adMatrix)]),
+    "bgpu_h5ad_read": (_i, [C.c_char_p, C.POINTER(H5adMatrix), _vp, _vp, _vp, _u32, _vp]),
 }
 
 _lock = threading.Lock()
@@ -175,6 +204,8 @@ def check(code: int, fn: str) -> None:
         msg = lib().bgpu_last_error().decode(errors="replace")
         if code == ERR_INVALID:
             raise ValueError(f"{fn}: {msg}")
+        if code == ERR_IO:
+            raise OSError(f"{fn}: {msg}")
         raise BriscGPUError(code, fn, msg)
 
 

@@ -27,6 +27,10 @@
  *   brisc/knn.pyx:13-515           knn_self                  -> bgpu_knn_self
  *   brisc/harmonize.pyx:244-266    normalize_rows            -> bgpu_normalize_rows
  *   brisc/harmonize.pyx:269-871    harmony                   -> bgpu_harmony
+ *   brisc/hdf5.pyx:163,
+ *   brisc/single_cell.py:1848-1883 h5py offsets + read_all_datasets
+ *                                                            -> bgpu_h5ad_inspect,
+ *                                                               bgpu_h5ad_read
  */
 #ifndef BRISCGPU_H
 #define BRISCGPU_H
@@ -51,7 +55,8 @@ enum {
   BGPU_ERR_ALLOC = 3,        /* device allocation failed                          */
   BGPU_ERR_UNSUPPORTED = 4,  /* input outside the supported layout limits         */
   BGPU_ERR_CANCELLED = 5,    /* the cancel flag was raised between restarts       */
-  BGPU_ERR_DEVICE = 6        /* a kernel reported an error status word            */
+  BGPU_ERR_DEVICE = 6,       /* a kernel reported an error status word            */
+  BGPU_ERR_IO = 7            /* reading a file failed                             */
 };
 
 /* ---- element types of caller arrays ------------------------------------ */
@@ -440,6 +445,47 @@ BGPU_API int bgpu_harmony(const float* PCs, float* Z, float* Y, float* R,
                           float sigma, uint32_t chunk_size, uint64_t seed,
                           uint64_t num_cells, uint32_t num_PCs, uint32_t num_clusters,
                           uint32_t* iterations, void* stream);
+
+/* ---- .h5ad count matrix straight to the device -------------------------- */
+/* The reference reads an AnnData file's sparse X by asking h5py for each
+ * dataset's byte offset (brisc/single_cell.py:1848-1883) and preading the
+ * contiguous bytes into host arrays with OpenMP threads (brisc/hdf5.pyx:163
+ * read_all_datasets). Here the HDF5 metadata is parsed by the library itself
+ * (no HDF5 library is needed) and the bytes go from the file through pinned
+ * staging buffers into device memory. */
+enum {  /* element types of index arrays in a file */
+  BGPU_H5_I32 = 0, BGPU_H5_I64 = 1, BGPU_H5_U32 = 2, BGPU_H5_U64 = 3
+};
+typedef struct bgpu_h5_dataset {
+  uint64_t file_offset;   /* byte offset of the contiguous storage in the file  */
+  uint64_t num_bytes;
+  uint64_t num_elements;
+  uint32_t element_size;
+  int type;               /* data: BGPU_VALUE_*; indices and indptr: BGPU_H5_* */
+} bgpu_h5_dataset;
+typedef struct bgpu_h5ad_matrix {
+  char X_key[64];         /* the group read: X_key, or the reference's choice   */
+  int is_csr;             /* encoding-type csr_matrix (1) or csc_matrix (0)     */
+  uint64_t num_rows, num_columns, nnz;  /* the shape attribute; stored entries */
+  bgpu_h5_dataset data, indices, indptr;
+} bgpu_h5ad_matrix;
+
+/* Parses the file's metadata and describes its sparse X: the group X_key, or
+ * (X_key NULL or "") 'layers/UMIs' when present, else 'raw/X', else 'X', as
+ * SingleCell's reader chooses (brisc/single_cell.py:497-522, 610-657), with
+ * its checks and messages (unsupported encoding-type, both layers['UMIs'] and
+ * raw.X, a corrupted indptr). Only contiguous, unfiltered datasets can be
+ * streamed (BGPU_ERR_UNSUPPORTED otherwise; the reference falls back to a
+ * slower reader there). Host only. */
+BGPU_API int bgpu_h5ad_inspect(const char* path, const char* X_key, bgpu_h5ad_matrix* out);
+/* Reads the three datasets `m` describes into device arrays (data:
+ * m->data.num_bytes bytes, and so on) with num_threads host threads (0 = all
+ * hardware threads), each preading 16 MB pieces into two pinned buffers of
+ * its own and copying them to the device while it reads the next. Waits for
+ * `stream` first; synchronous. */
+BGPU_API int bgpu_h5ad_read(const char* path, const bgpu_h5ad_matrix* m, void* data,
+                            void* indices, void* indptr, uint32_t num_threads,
+                            void* stream);
 
 #ifdef __cplusplus
 }

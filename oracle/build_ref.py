@@ -44,11 +44,11 @@ HERE = Path(__file__).resolve().parent
 REF_OUT = HERE / "_ref"
 GEN = REF_OUT / "gen"
 MODULES = ["cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn",
-           "harmonize"]
+           "harmonize", "hdf5"]
 # What the CPU baselines need (cysparse's 24 MB of C++ is only needed for the
 # transpose fixture and is skipped where compile time matters).
 BASELINE_MODULES = ["cyutils", "pca", "normalize", "hvg", "kmeans", "knn",
-                    "harmonize", "ref_probe"]
+                    "harmonize", "hdf5", "ref_probe"]
 DIRECTIVES = {"language_level": "3", "boundscheck": False,
               "wraparound": False, "cdivision": True,
               "initializedcheck": False, "warn.undeclared": False}

@@ -58,11 +58,11 @@ def load(build: bool = True):
         sys.path.insert(0, str(d))
     _mods = {}
     for name in ("cyutils", "pca", "normalize", "cysparse", "hvg", "kmeans", "knn",
-                 "harmonize", "ref_probe"):
+                 "harmonize", "hdf5", "ref_probe"):
         try:
             _mods[name] = importlib.import_module(f"brisc.{name}")
         except ImportError:
-            if name not in ("cysparse", "hvg", "kmeans", "knn", "harmonize"):
+            if name not in ("cysparse", "hvg", "kmeans", "knn", "harmonize", "hdf5"):
                 raise
     return _mods
 
@@ -305,3 +305,25 @@ def run_harmonize(PCs, batch_labels, num_batches: int, num_clusters=None,
                   num_threads=num_threads)
     return dict(Z=Z, R=R, Y_init=Y_init, Y=Y, kmeans_iterations=km["iterations"],
                 num_clusters=num_clusters)
+
+
+def run_read_all_datasets(path, datasets, num_threads: int | None = None):
+    """The reference's contiguous-dataset reader (brisc/hdf5.pyx:163
+    read_all_datasets) as SingleCell._read_parallel calls it for large
+    fixed-width datasets (brisc/single_cell.py:1964-2200): one pread slice per
+    thread of every dataset, into NumPy arrays. ``datasets`` is a list of
+    (file_offset, dtype, num_elements); the offsets come from the caller (the
+    reference gets them from h5py, absent here). Returns the arrays."""
+    M = load()
+    H = M["hdf5"]
+    num_threads = num_threads or os.cpu_count() or 1
+    arrays = [np.empty(int(n), dtype=dt) for _, dt, n in datasets]
+    u64 = lambda v: np.asarray(v, dtype=np.uint64)  # noqa: E731
+    fd = os.open(path, os.O_RDONLY)
+    try:
+        H.read_all_datasets(
+            fd, arrays, u64([off for off, _, _ in datasets]), u64([]), u64([]), u64([]),
+            u64([0] * (num_threads + 1)), u64([]), u64([]), 8, 8, num_threads)
+    finally:
+        os.close(fd)
+    return arrays

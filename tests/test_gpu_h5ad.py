@@ -1,0 +1,63 @@
+"""X of an .h5ad file streamed to the device (bgpu_h5ad_read,
+brisc_gb300/h5ad.py): the device arrays hold exactly the written bytes
+(several 16 MB pieces, several threads, both HDF5 layouts), and the PCA from
+the file-built DeviceMatrix is bit-identical to the one built from host
+arrays (CSR and CSC files)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import h5file
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("style,threads", [("v0", 0), ("v2", 3), ("v0", 1)])
+def test_read_X_bit_exact(cuda, tmp_path, style, threads):
+    from brisc_gb300 import h5ad
+    rng = np.random.default_rng(4)
+    nnz = 6_000_017  # 24 MB of float32: two pieces, a ragged tail
+    n, g = 40_000, 3000
+    indptr = np.sort(rng.integers(0, nnz + 1, n + 1)).astype(np.int64)
+    indptr[0], indptr[-1] = 0, nnz
+    indices = rng.integers(0, g, nnz).astype(np.int32)
+    data = rng.random(nnz, dtype=np.float32)
+    path = str(tmp_path / "big.h5ad")
+    h5file.write_h5ad(path, data, indices, indptr, (n, g), style=style)
+    X = h5ad.read_X(path, num_threads=threads)
+    assert X["shape"] == (n, g) and X["format"] == "csr"
+    np.testing.assert_array_equal(X["data"].cpu().numpy(), data)
+    np.testing.assert_array_equal(X["indices"].cpu().numpy(), indices)
+    np.testing.assert_array_equal(X["indptr"].cpu().numpy(), indptr)
+
+
+def test_read_X_empty_matrix(cuda, tmp_path):
+    from brisc_gb300 import h5ad
+    path = str(tmp_path / "empty.h5ad")
+    h5file.write_h5ad(path, np.zeros(0, np.float32), np.zeros(0, np.int32),
+                      np.zeros(11, np.int64), (10, 5))
+    X = h5ad.read_X(path)
+    assert X["data"].numel() == 0 and X["indptr"].cpu().numpy().tolist() == [0] * 11
+
+
+@pytest.mark.parametrize("fmt", ["csr_matrix", "csc_matrix"])
+def test_device_matrix_pca_matches_host_arrays(cuda, tmp_path, fmt):
+    from synth import nb_counts
+    from brisc_gb300 import h5ad
+    from brisc_gb300.pca import DeviceMatrix, size_factors
+    C = nb_counts(4000, 600, seed=5, density=0.08, workers=1)
+    X = sp.csr_matrix((C.data.astype(np.float32), C.indices.astype(np.int32),
+                       C.indptr.astype(np.int64)), shape=(C.num_cells, C.num_genes))
+    S = X if fmt == "csr_matrix" else X.tocsc()
+    path = str(tmp_path / "pbmc.h5ad")
+    h5file.write_h5ad(path, S.data, S.indices.astype(np.int32), S.indptr.astype(np.int64),
+                      X.shape, fmt=fmt)
+    M = h5ad.device_matrix(path, method="logCP10k")
+    a = M.solve(10, 20, 1e-6, 100, 0, 1024).PCs
+    isf, _ = size_factors(X, "logCP10k")
+    H = DeviceMatrix(X.indptr.astype(np.int32), X.indices, X.data, X.shape[0], X.shape[1],
+                     norm="logCP10k", inv_size_factors=isf)
+    b = H.solve(10, 20, 1e-6, 100, 0, 1024).PCs
+    M.close()
+    H.close()
+    np.testing.assert_array_equal(a, b)
