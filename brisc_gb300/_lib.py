@@ -107,6 +107,7 @@ class HvgInput(C.Structure):
 
 
 H5_I32, H5_I64, H5_U32, H5_U64 = 0, 1, 2, 3  # index arrays in an .h5ad file
+H5_READ = {"auto": 0, "staged": 1, "mapped": 2}
 
 
 class H5Dataset(C.Structure):
@@ -168,7 +169,8 @@ SIGNATURES = {
     "bgpu_harmony": (_i, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _u32, _f, _f, _i, _f, _f,
                           _f, _f, _f, _u32, _u64, _u64, _u32, _u32, C.POINTER(_u32), _vp]),
     "bgpu_h5ad_inspect": (_i, [C.c_char_p, C.c_char_p, C.POINTER(H5adMatrix)]),
-    "bgpu_h5ad_read": (_i, [C.c_char_p, C.POINTER(H5adMatrix), _vp, _vp, _vp, _u32, _vp]),
+    "bgpu_h5ad_read": (_i, [C.c_char_p, C.POINTER(H5adMatrix), _vp, _vp, _vp, _u32, _u32,
+                            _vp]),
 }
 
 _lock = threading.Lock()

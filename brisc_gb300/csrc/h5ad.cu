@@ -24,6 +24,7 @@
 // 'h5sparse_format' + '_matrix'; the shape from 'shape', else
 // 'h5sparse_shape'.
 #include <fcntl.h>
+#include <sys/mman.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -714,7 +715,7 @@ int inspect(const char* path, const char* X_key, bgpu_h5ad_matrix* out) {
 
 // ---------------------------------------------------------------------------
 // streaming reader
-constexpr uint64_t kPiece = 16ull << 20;  // bytes per pread / copy
+constexpr uint64_t kPiece = 4ull << 20;  // bytes per pread / copy
 constexpr int kMaxThreads = 64;
 
 struct Staging {
@@ -841,16 +842,88 @@ extern "C" int bgpu_h5ad_inspect(const char* path, const char* X_key, bgpu_h5ad_
   }
 }
 
+// Zero-copy: the byte range of the three datasets mapped read-only and
+// registered with the driver (cudaHostRegisterReadOnly, the registration made
+// for read-only file mappings), so the copy engines read the page-cache pages
+// directly and no host thread copies a byte. *refused is set (and nothing is
+// copied) when the mapping or the registration is not possible here.
+int read_mapped(const char* path, const bgpu_h5_dataset* const ds[3], void* const dst[3],
+                cudaStream_t s, bool* refused) {
+  *refused = true;
+  int dev = 0, ro = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ro, cudaDevAttrHostRegisterReadOnlySupported, dev) !=
+          cudaSuccess || !ro) {
+    cudaGetLastError();
+    return BGPU_OK;
+  }
+  uint64_t lo = ~0ull, hi = 0;
+  for (int q = 0; q < 3; ++q)
+    if (ds[q]->num_bytes) {
+      lo = std::min(lo, ds[q]->file_offset);
+      hi = std::max(hi, ds[q]->file_offset + ds[q]->num_bytes);
+    }
+  if (hi == 0) {
+    *refused = false;
+    return BGPU_OK;
+  }
+  const int fd = ::open(path, O_RDONLY);
+  BGPU_REQUIRE(fd >= 0, BGPU_ERR_IO, std::string("cannot open ") + path);
+  const off_t fsize = ::lseek(fd, 0, SEEK_END);
+  if (fsize < 0 || (uint64_t)fsize < hi) {
+    ::close(fd);
+    BGPU_REQUIRE(false, BGPU_ERR_IO, "the .h5ad file ends before its data");
+  }
+  const uint64_t page = (uint64_t)sysconf(_SC_PAGESIZE);
+  const uint64_t start = lo & ~(page - 1), len = hi - start;
+  void* map = ::mmap(nullptr, len, PROT_READ, MAP_SHARED, fd, (off_t)start);
+  if (map == MAP_FAILED) {
+    ::close(fd);
+    return BGPU_OK;
+  }
+  if (cudaHostRegister(map, len, cudaHostRegisterReadOnly) != cudaSuccess) {
+    cudaGetLastError();
+    ::munmap(map, len);
+    ::close(fd);
+    return BGPU_OK;
+  }
+  *refused = false;
+  int rc = BGPU_OK;
+  cudaError_t e = cudaStreamSynchronize(s);  // the caller's earlier work first
+  for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+    if (ds[q]->num_bytes)
+      e = cudaMemcpyAsync(dst[q], (const char*)map + (ds[q]->file_offset - start),
+                          ds[q]->num_bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_error(std::string("copying the mapped .h5ad data failed: ") + cudaGetErrorString(e));
+    rc = BGPU_ERR_CUDA;
+  }
+  cudaHostUnregister(map);
+  ::munmap(map, len);
+  ::close(fd);
+  return rc;
+}
+
 extern "C" int bgpu_h5ad_read(const char* path, const bgpu_h5ad_matrix* m, void* data,
-                              void* indices, void* indptr, uint32_t num_threads,
-                              void* stream) {
+                              void* indices, void* indptr, uint32_t method,
+                              uint32_t num_threads, void* stream) {
   BGPU_REQUIRE(path && m, BGPU_ERR_INVALID, "h5ad: NULL argument");
+  BGPU_REQUIRE(method <= BGPU_H5_READ_MAPPED, BGPU_ERR_INVALID, "h5ad: unknown read method");
   const bgpu_h5_dataset* ds[3] = {&m->data, &m->indices, &m->indptr};
   void* dst[3] = {data, indices, indptr};
-  std::vector<Piece> pieces;
-  for (int q = 0; q < 3; ++q) {
+  for (int q = 0; q < 3; ++q)
     BGPU_REQUIRE(ds[q]->num_bytes == 0 || dst[q], BGPU_ERR_INVALID,
                  "h5ad: NULL destination for a non-empty dataset");
+  if (method != BGPU_H5_READ_STAGED) {
+    bool refused = true;
+    BGPU_TRY(read_mapped(path, ds, dst, (cudaStream_t)stream, &refused));
+    if (!refused) return BGPU_OK;
+    BGPU_REQUIRE(method != BGPU_H5_READ_MAPPED, BGPU_ERR_UNSUPPORTED,
+                 "h5ad: the file cannot be mapped and registered with the driver here");
+  }
+  std::vector<Piece> pieces;
+  for (int q = 0; q < 3; ++q) {
     for (uint64_t o = 0; o < ds[q]->num_bytes; o += kPiece)
       pieces.push_back({ds[q]->file_offset + o, std::min(kPiece, ds[q]->num_bytes - o),
                         (char*)dst[q] + o});

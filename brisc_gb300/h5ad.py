@@ -61,11 +61,14 @@ def _torch_dtype(name: str):
 
 
 def read_X(path, X_key: str | None = None, num_threads: int = 0, device=None,
-           stream=None) -> dict:
+           stream=None, method: str = "auto") -> dict:
     """X's three arrays as CUDA tensors (element types as stored; unsigned
     index arrays come back as the signed type of the same width, holding the
     same bits), plus ``shape``, ``format`` ('csr' or 'csc') and ``X_key``.
-    ``num_threads`` host threads read (0: all)."""
+    ``method``: 'mapped' (the file range registered with the driver, copied
+    by the copy engines straight from the page cache), 'staged' (``num_threads``
+    host threads, 0 = all, pread into pinned buffers) or 'auto' (mapped
+    where the driver allows it)."""
     import torch
     m = _info(path, X_key)
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None \
@@ -84,7 +87,8 @@ def read_X(path, X_key: str | None = None, num_threads: int = 0, device=None,
         L.call("bgpu_h5ad_read", os.fsencode(path), C.byref(m),
                out["data"].data_ptr() if out["data"].numel() else None,
                out["indices"].data_ptr() if out["indices"].numel() else None,
-               out["indptr"].data_ptr(), int(num_threads), C.c_void_p(s.cuda_stream))
+               out["indptr"].data_ptr(), L.H5_READ[method], int(num_threads),
+               C.c_void_p(s.cuda_stream))
     out.update(shape=(int(m.num_rows), int(m.num_columns)),
                format="csr" if m.is_csr else "csc", X_key=m.X_key.decode())
     return out

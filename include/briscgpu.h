@@ -478,14 +478,21 @@ typedef struct bgpu_h5ad_matrix {
  * streamed (BGPU_ERR_UNSUPPORTED otherwise; the reference falls back to a
  * slower reader there). Host only. */
 BGPU_API int bgpu_h5ad_inspect(const char* path, const char* X_key, bgpu_h5ad_matrix* out);
+enum {
+  BGPU_H5_READ_AUTO = 0,    /* mapped where the driver allows it, else staged   */
+  BGPU_H5_READ_STAGED = 1,  /* host threads pread into pinned buffers and copy  */
+  BGPU_H5_READ_MAPPED = 2   /* the file range mapped read-only and registered
+                               (cudaHostRegisterReadOnly): the copy engines read
+                               the page cache directly; UNSUPPORTED if refused  */
+};
 /* Reads the three datasets `m` describes into device arrays (data:
- * m->data.num_bytes bytes, and so on) with num_threads host threads (0 = all
- * hardware threads), each preading 16 MB pieces into two pinned buffers of
- * its own and copying them to the device while it reads the next. Waits for
- * `stream` first; synchronous. */
+ * m->data.num_bytes bytes, and so on). Staged: num_threads host threads (0 =
+ * all hardware threads) each pread 4 MB pieces into two pinned buffers of its
+ * own and copy them to the device while reading the next. Waits for `stream`
+ * first; synchronous. */
 BGPU_API int bgpu_h5ad_read(const char* path, const bgpu_h5ad_matrix* m, void* data,
-                            void* indices, void* indptr, uint32_t num_threads,
-                            void* stream);
+                            void* indices, void* indptr, uint32_t method,
+                            uint32_t num_threads, void* stream);
 
 #ifdef __cplusplus
 }
