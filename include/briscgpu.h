@@ -297,9 +297,10 @@ BGPU_API int bgpu_small_svd(const float* B, uint32_t m, float* Ub, float* Sb,
  * the reference (its sgesdd call allocates host workspace, pca.pyx:514-528).
  * Allocates nothing: its scratch is a fixed device array inside the library
  * (about 1.6 MB per GPU that loads it, held until exit). m <= 256, else
- * BGPU_ERR_INVALID. The first call on each device looks the array up; make it
- * before any stream capture. Calls share the array: two whose work overlaps on
- * the GPU race. Returns after the SVD has completed on `stream`. */
+ * BGPU_ERR_INVALID. The first call on each device looks the array up. Calls
+ * share the array: two whose work overlaps on the GPU race. The call
+ * synchronises `stream` before it returns (the SVD has completed), so it
+ * cannot be captured into a CUDA graph. */
 BGPU_API int bgpu_small_svd_noalloc(const float* B, uint32_t m, float* Ub,
                                     float* Sb, float* Vbt, void* stream);
 

@@ -41,8 +41,9 @@ def _svd(fn, Bf, m, dev):
             Vbt.cpu().numpy().reshape(m, m + 1, order="F"))
 
 
-# 100: matrices in shared memory; 200: Jacobi workspace in the scratch array
-@pytest.mark.parametrize("m", [100, 200])
+# 100: matrices in shared memory; 200: Jacobi workspace in the scratch array;
+# 256: the largest m, whose workspace fills the fixed scratch array exactly
+@pytest.mark.parametrize("m", [100, 200, 256])
 def test_noalloc_small_svd_matches_allocating_entry(cuda, m):
     for call, seed in enumerate((11, 12)):  # two calls in a row, new input each
         Bf = _irlba_like_b(m, seed + m)
