@@ -57,6 +57,8 @@ namespace {
 constexpr int kTcThreads = 512;
 constexpr int kTcRows = 128;  // M of one MMA / rows per tile
 constexpr uint32_t kTcChunkK = 112;  // K per staging (A and B halves in smem)
+// the per-task packing of k_gemm_tc: <= 16 k groups, offsets below 2^16
+static_assert(kTcChunkK <= 128, "k_gemm_tc packs k groups and offsets in 16 bits");
 constexpr uint32_t kTcChunkN = 128;  // output columns per staging
 constexpr uint32_t kTcMaxK = 1024;
 
@@ -198,6 +200,7 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
   __shared__ int stop;
   __shared__ int spiv[kTcChunkN];  // pivot of each output column (0: none)
+  __shared__ long long spoff[kTcChunkN];  // its source column's offset (-1: none)
   const TcLayout L(Kp, Np);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const uint32_t kq = Kp / 8;  // 16-byte K groups (8 BF16) per row
@@ -215,8 +218,11 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     fence_mbar_init();
     stop = 0;
   }
-  for (uint32_t c = tid; c < kTcChunkN; c += kTcThreads)
-    spiv[c] = (piv && c < ncols) ? piv[c] : 0;
+  for (uint32_t c = tid; c < kTcChunkN; c += kTcThreads) {
+    const int pv = (piv && c < ncols) ? piv[c] : 0;
+    spiv[c] = pv;
+    spoff[c] = pv == 0 ? -1ll : (long long)(pv > 0 ? pv - 1 : -pv - 1) * (long long)lda;
+  }
   // B operand (N x K, K-major): row n of it is column n of Bm.
   for (uint32_t t = tid; t < Np * kq; t += kTcThreads) {
     const uint32_t n = t / kq, kg = t % kq;
@@ -242,18 +248,32 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
 
   // A tile values of one tile, in registers: task = (row group, k group, row
   // in group); 8 lanes read 8 consecutive rows of one column (32-byte runs).
+  // A task's k group, row and destination are the same for every tile:
+  // computed once and packed (bits 0-15 shared-memory offset, 16-19 k group,
+  // 20-23 valid k count, 24-30 row in the tile; no task: 0xFFFFFFFF).
   float xa[kTcTasks][8];
+  uint32_t t_meta[kTcTasks];
+#pragma unroll
+  for (int i = 0; i < kTcTasks; ++i) {
+    const uint32_t t = tid + i * kTcThreads;
+    const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
+    const uint32_t nk = kg * 8 >= K ? 0u : min(8u, K - kg * 8);
+    t_meta[i] = t < ntask ? core_off(rg * 8 + rr, kg, kq) | (kg << 16) | (nk << 20) |
+                                ((rg * 8 + rr) << 24)
+                          : 0xFFFFFFFFu;
+  }
   auto load_tile = [&](uint64_t row0) {
+    const bool full = row0 + kTcRows <= rows;
 #pragma unroll
     for (int i = 0; i < kTcTasks; ++i) {
-      const uint32_t t = tid + i * kTcThreads;
-      const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
-      const uint64_t gr = row0 + rg * 8 + rr;
+      const uint32_t meta = t_meta[i];
+      const uint32_t nk = meta == 0xFFFFFFFFu ? 0u : (meta >> 20) & 15u;
+      const uint32_t row = (meta >> 24) & 127u;
+      const float* src = A + (uint64_t)(((meta >> 16) & 15u) * 8u) * lda + row0 + row;
+      const bool rok = full || row0 + row < rows;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const uint32_t k = kg * 8 + j;
-        xa[i][j] = (t < ntask && gr < rows && k < K) ? A[(uint64_t)k * lda + gr] : 0.f;
-      }
+      for (int j = 0; j < 8; ++j)
+        xa[i][j] = (rok && (uint32_t)j < nk) ? src[(uint64_t)j * lda] : 0.f;
     }
   };
 
@@ -268,14 +288,16 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   float pa[32];                     // signed pivot values of this thread's row
   auto prefetch_pivots = [&](uint64_t row0) {
     const uint64_t gr = row0 + q * 32 + lane;
+    const bool rok = gr < rows;
+    const float* ap = Apiv + gr;
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
-      const uint32_t c = h * quarter + j;
-      const int pv = (j < (int)quarter && c < ncols) ? spiv[c] : 0;
+      const uint32_t c = h * quarter + j;  // < 128: spoff / spiv cover it
+      const long long off = spoff[c];
       float a = 0.f;
-      if (pv != 0 && gr < rows) {
-        a = Apiv[(uint64_t)(pv > 0 ? pv - 1 : -pv - 1) * lda + gr];
-        if (pv < 0) a = -a;
+      if ((uint32_t)j < quarter && off >= 0 && rok) {
+        a = ap[off];
+        if (spiv[c] < 0) a = -a;
       }
       pa[j] = a;
     }
@@ -284,21 +306,20 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   // of quarter w/4; lane = row.
   auto epilogue = [&](uint64_t row0, uint32_t acc) {
     const uint64_t gr = row0 + q * 32 + lane;
+    float* cp = C + (uint64_t)(h * quarter) * ldc + gr;  // column h * quarter
 #pragma unroll
     for (uint32_t g8 = 0; g8 < 4; ++g8) {
       const uint32_t c0 = h * quarter + g8 * 8;
       if (g8 * 8 >= quarter) break;
       float v[8];
       tmem_ld8(acc + ((q * 32u) << 16) + c0, v);
-      if (gr < rows) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (c0 + j < ncols) {
-            const float val = v[j] + pa[g8 * 8 + j];  // pivot column, FP32 add
-            float* cp = C + (uint64_t)(c0 + j) * ldc + gr;
-            *cp = accumulate ? *cp + val : val;  // K chunks add in order
-          }
+      for (int j = 0; j < 8; ++j) {
+        if (gr < rows && c0 + j < ncols) {
+          const float val = v[j] + pa[g8 * 8 + j];  // pivot column, FP32 add
+          *cp = accumulate ? *cp + val : val;  // K chunks add in order
         }
+        cp += ldc;
       }
     }
   };
@@ -322,15 +343,13 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
     if (has_cur) {
 #pragma unroll
       for (int i = 0; i < kTcTasks; ++i) {
-        const uint32_t t = tid + i * kTcThreads;
-        if (t < ntask) {
-          const uint32_t rr = t & 7u, kg = (t >> 3) % kq, rg = (t >> 3) / kq;
+        if (t_meta[i] != 0xFFFFFFFFu) {
+          const uint32_t off = t_meta[i] & 0xFFFFu;
           uint4 p[3];
           split8(xa[i], p);
 #pragma unroll
           for (int part = 0; part < 3; ++part)
-            *reinterpret_cast<uint4*>(smem + L.a[part] + core_off(rg * 8 + rr, kg, kq)) =
-                p[part];
+            *reinterpret_cast<uint4*>(smem + L.a[part] + off) = p[part];
         }
       }
       fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
