@@ -42,6 +42,13 @@
 // the previous tile's accumulator (tcgen05.ld, 32 lanes x 8 columns per
 // load) and store C column-major (128-byte runs per column).
 //
+// Subspaces beyond one staging (K > 112: the 10M-cell solve's m = 200) run
+// in k_gemm_tc_pipe, which keeps B resident and streams A in K chunks of 16
+// to 32 through a warp-specialised pipeline (producer warps: cp.async ring,
+// split, stage; one MMA lane; epilogue warps), the small cross products and
+// x1y1 in separate accumulators added in FP32 in the epilogue; output columns
+// in chunks of 128.
+//
 // Every mbarrier wait is bounded (about 1 s of SM clock): on timeout the
 // kernel records kDevErrTimeout, stops, frees its TMEM and returns.
 #include <algorithm>
@@ -60,7 +67,6 @@ constexpr uint32_t kTcChunkK = 112;  // K per staging (A and B halves in smem)
 // the per-task packing of k_gemm_tc: <= 16 k groups, offsets below 2^16
 static_assert(kTcChunkK <= 128, "k_gemm_tc packs k groups and offsets in 16 bits");
 constexpr uint32_t kTcChunkN = 128;  // output columns per staging
-constexpr uint32_t kTcMaxK = 1024;
 
 struct TcLayout {  // three BF16 parts of the A tile and of B
   uint32_t a[3], b[3], total;
@@ -151,6 +157,50 @@ __device__ __forceinline__ void split8(const float (&x)[8], uint4 (&p)[3]) {
 __device__ __forceinline__ uint32_t core_off(uint32_t row, uint32_t kg, uint32_t kq) {
   return ((row >> 3) * kq + kg) * 128u + (row & 7u) * 16u;
 }
+
+// 16 columns of two accumulators (lane = row), one wait for all 32 values.
+__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float (&va)[16],
+                                            float (&vb)[16]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+      "%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+        "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(ta)
+      : "memory");
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+      "%12,%13,%14,%15}, [%16];"
+      : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(tb)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    va[i] = __uint_as_float(r[i]);
+    vb[i] = __uint_as_float(r[16 + i]);
+  }
+}
+
+// 16-byte asynchronous copy global -> shared, src_bytes (0-16) read and the
+// rest zero-filled; both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 
 // Tasks per thread when a tile's A values are staged in registers: one task
 // is 8 consecutive k of one row (128 rows x Kp/8 tasks, Kp <= 112).
@@ -405,10 +455,348 @@ k_gemm_tc(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// The pipelined rotation (K > 112).
+constexpr int kTpRows = 128;          // M of one MMA / rows per tile
+constexpr int kTpProducerWarps = 8;   // load, split and stage tiles of U
+constexpr int kTpMmaWarp = kTpProducerWarps;  // one lane issues the MMAs
+constexpr int kTpEpilogueWarps = 4;   // drain TMEM, one per 32-lane quarter
+constexpr int kTpThreads = 32 * (kTpProducerWarps + 1 + kTpEpilogueWarps);
+constexpr int kTpProducerThreads = 32 * kTpProducerWarps;
+constexpr int kTpTasks = 2;           // 8-value split tasks per producer thread and chunk
+constexpr uint32_t kTpChunkN = 128;   // output columns per launch: four accumulators
+constexpr uint32_t kTpMaxKc = 32;     // K per staged chunk of a tile
+constexpr int kTpRing = 4;            // FP32 chunks in flight (cp.async ring)
+constexpr uint32_t kTpMaxK = 1024;
+constexpr size_t kTpSmem = 227 * 1024;
+static_assert(kTpRows * kTpMaxKc / 8 <= kTpTasks * kTpProducerThreads,
+              "a chunk's split tasks fit the producer threads");
+
+// Shared memory: barriers and the TMEM slot, B's three BF16 parts (resident),
+// two buffers of the A chunk's three BF16 parts (K-major core matrices, read
+// by the MMAs), and a ring of FP32 A chunks ([k][row], filled by cp.async).
+struct TpLayout {
+  uint32_t b[3], a[2][3], f[kTpRing], total;
+  __host__ __device__ TpLayout(uint32_t Kp, uint32_t Np, uint32_t KC) {
+    uint32_t o = 1024;
+    for (int i = 0; i < 3; ++i) {
+      b[i] = o;
+      o += Np * Kp * 2;
+    }
+    for (int st = 0; st < 2; ++st)
+      for (int i = 0; i < 3; ++i) {
+        a[st][i] = o;
+        o += kTpRows * KC * 2;
+      }
+    for (int r = 0; r < kTpRing; ++r) {
+      f[r] = o;
+      o += kTpRows * KC * 4;
+    }
+    total = o;
+  }
+};
+
+// The producer warps' own barrier (named barrier 1).
+__device__ __forceinline__ void producers_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kTpProducerThreads) : "memory");
+}
+
+// Bounded wait for phase `parity` of `bar` that gives up when another role has
+// raised *stop; a timeout (~2^31 SM cycles) records the error word and
+// raises *stop.
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* stop,
+                                        int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (true) {
+    if (*stop) return false;
+    if (mbar_try_wait(bar, parity)) return true;
+    if (clock64() - t0 > (2LL << 30)) {
+      atomicOr(err, kDevErrTimeout);
+      *stop = 1;
+      return false;
+    }
+  }
+}
+
+// C = A . Bm, plus sign Apiv[:, p] for the columns with a pivot (piv may be
+// null). Warp-specialised and pipelined: producer warps load a K chunk of a
+// 128-row tile of A, split it and stage it in one of two shared buffers; the
+// MMA lane issues that chunk's MMAs (the five small cross products into one
+// accumulator, x1y1 into another) and commits; epilogue warps add the two
+// accumulators and the pivot column in FP32 and store C, while the next
+// tile's MMAs run into the other accumulator pair. mbarriers: a_full
+// (producers -> MMA), a_empty (MMA commit -> producers), acc_full (MMA commit
+// -> epilogue), acc_empty (epilogue -> MMA). Waits are bounded; a timeout
+// records the error word, raises a stop flag every waiting role polls, and
+// the MMA lane waits (bounded) for its last commit before TMEM is freed.
+__global__ void __launch_bounds__(kTpThreads, 1)
+k_gemm_tc_pipe(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_t K,
+          const float* __restrict__ Bm, uint64_t ldb, uint32_t ncols,
+          float* __restrict__ C, uint64_t ldc, uint32_t Kp, uint32_t Np, uint32_t KC,
+          uint32_t tmem_cols, int accumulate, const float* __restrict__ Apiv,
+          const int* __restrict__ piv, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* a_full = bars;         // [2], one arrive per producer warp
+  uint64_t* a_empty = bars + 2;    // [2], MMA commit
+  uint64_t* acc_full = bars + 4;   // [2], MMA commit
+  uint64_t* acc_empty = bars + 6;  // [2], one arrive per epilogue warp
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 128);
+  __shared__ volatile int stop;
+  __shared__ int spiv[kTpChunkN];         // pivot of each output column (0: none)
+  __shared__ long long spoff[kTpChunkN];  // its source column's offset (-1: none)
+  const TpLayout L(Kp, Np, KC);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t kq = Kp / 8;  // B's 16-byte K groups per row
+  const uint32_t nch = (Kp + KC - 1) / KC;
+
+  if (wid == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_u32(tslot)), "r"(4u * tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(a_full + b, kTpProducerWarps);
+      mbar_init(a_empty + b, 1);
+      mbar_init(acc_full + b, 1);
+      mbar_init(acc_empty + b, kTpEpilogueWarps);
+    }
+    fence_mbar_init();
+    stop = 0;
+  }
+  for (uint32_t c = tid; c < kTpChunkN; c += kTpThreads) {
+    const int pv = (piv && c < ncols) ? piv[c] : 0;
+    spiv[c] = pv;
+    spoff[c] = pv == 0 ? -1ll : (long long)(pv > 0 ? pv - 1 : -pv - 1) * (long long)lda;
+  }
+  // B operand (N x K, K-major): row n of it is column n of Bm.
+  for (uint32_t t = tid; t < Np * kq; t += kTpThreads) {
+    const uint32_t n = t / kq, kg = t % kq;
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t k = kg * 8 + j;
+      x[j] = (n < ncols && k < K) ? Bm[(uint64_t)n * ldb + k] : 0.f;
+    }
+    uint4 p[3];
+    split8(x, p);
+#pragma unroll
+    for (int part = 0; part < 3; ++part)
+      *reinterpret_cast<uint4*>(smem + L.b[part] + core_off(n, kg, kq)) = p[part];
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint64_t ntiles = (rows + kTpRows - 1) / kTpRows;
+  const uint64_t my_tiles =
+      blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+
+  auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
+    return tc_wait(bar, parity, &stop, err);
+  };
+
+  if (wid < kTpProducerWarps) {
+    // ---- producers: stage s = (tile ti, chunk c), BF16 buffer s & 1 --------
+    // Each chunk (KC columns of 128 rows of A) is copied with cp.async into
+    // ring slot s % kTpRing, kTpRing - 1 chunks ahead; then split from there
+    // (task = 8 consecutive k of one row) into the BF16 buffer. Decisions that
+    // end the loop are taken by thread 0 and shared through the producers'
+    // barrier, so every producer thread reaches every barrier.
+    __shared__ int pgo;
+    const uint32_t wf = KC / 8, wl = (Kp - (nch - 1) * KC) / 8;
+    uint32_t mf[kTpTasks], ml[kTpTasks];  // row | k group << 8 | 1 << 16 (0: none)
+#pragma unroll
+    for (int i = 0; i < kTpTasks; ++i) {
+      const uint32_t t = tid + i * kTpProducerThreads;
+      mf[i] = t < kTpRows * wf ? (((t >> 3) / wf) * 8 + (t & 7u)) | (((t >> 3) % wf) << 8) |
+                                     (1u << 16)
+                               : 0u;
+      ml[i] = t < kTpRows * wl ? (((t >> 3) / wl) * 8 + (t & 7u)) | (((t >> 3) % wl) << 8) |
+                                     (1u << 16)
+                               : 0u;
+    }
+    const uint64_t S = my_tiles * nch;
+    auto issue = [&](uint64_t st) {  // ring slot st % kTpRing <- chunk st
+      const uint64_t ti = st / nch;
+      const uint32_t c = (uint32_t)(st % nch);
+      const uint64_t row0 = (blockIdx.x + ti * gridDim.x) * kTpRows;
+      float* ring = reinterpret_cast<float*>(smem + L.f[st % kTpRing]);
+      const uint32_t w = min(KC, Kp - c * KC);
+      for (uint32_t e = tid; e < w * 32u; e += kTpProducerThreads) {
+        const uint32_t kl = e >> 5, r4 = (e & 31u) * 4u;
+        const uint32_t k = c * KC + kl;
+        const uint64_t gr = row0 + r4;
+        const uint32_t nb = (k < K && gr < rows) ? (uint32_t)min_u64(16, (rows - gr) * 4) : 0u;
+        cp_async16(ring + kl * kTpRows + r4, nb ? A + (uint64_t)k * lda + gr : A, nb);
+      }
+    };
+    for (int s0 = 0; s0 < kTpRing - 1; ++s0) {
+      if ((uint64_t)s0 < S) issue(s0);
+      cp_async_commit();
+    }
+    for (uint64_t st = 0; st < S; ++st) {
+      if (st + kTpRing - 1 < S) issue(st + kTpRing - 1);
+      cp_async_commit();
+      cp_async_wait<kTpRing - 1>();  // this thread's copies of chunk st landed
+      const uint32_t b = (uint32_t)(st & 1u);
+      if (tid == 0)
+        pgo = (st < 2 || wait(a_empty + b, (uint32_t)(((st >> 1) - 1) & 1u))) ? 1 : 0;
+      producers_sync();  // every copy of chunk st visible; BF16 buffer b free
+      if (!pgo) break;
+      const uint32_t c = (uint32_t)(st % nch);
+      const bool last = c == nch - 1;
+      const uint32_t wq = last ? wl : wf;
+      const float* ring = reinterpret_cast<const float*>(smem + L.f[st % kTpRing]);
+#pragma unroll
+      for (int i = 0; i < kTpTasks; ++i) {
+        const uint32_t m = last ? ml[i] : mf[i];
+        if (m) {
+          const uint32_t row = m & 255u, kg = (m >> 8) & 255u;
+          float x[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) x[j] = ring[(kg * 8 + j) * kTpRows + row];
+          uint4 p[3];
+          split8(x, p);
+          const uint32_t off = core_off(row, kg, wq);
+#pragma unroll
+          for (int part = 0; part < 3; ++part)
+            *reinterpret_cast<uint4*>(smem + L.a[b][part] + off) = p[part];
+        }
+      }
+      fence_proxy_async_smem();  // generic-proxy writes -> tensor-core reads
+      __syncwarp();
+      if (lane == 0) mbar_arrive(a_full + b);
+      producers_sync();  // ring slot st % kTpRing is read: it may be refilled
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy outlives the CTA
+  } else if (wid == kTpMmaWarp) {
+    // ---- MMA lane --------------------------------------------------------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(kTpRows, Np);
+      const uint32_t sbo_b = kq * 128u;
+      const uint32_t base = smem_u32(smem);
+      uint64_t* last_bar = nullptr;
+      uint32_t last_par = 0;
+      uint64_t st = 0;
+      bool ok = true;
+      for (uint64_t i = 0; i < my_tiles && ok; ++i) {
+        const uint32_t ab = (uint32_t)(i & 1u);
+        const uint32_t acc_s = tmem + 2u * ab * tmem_cols, acc_b = acc_s + tmem_cols;
+        if (i >= 2 && !wait(acc_empty + ab, (uint32_t)(((i >> 1) - 1) & 1u))) break;
+        for (uint32_t c = 0; c < nch; ++c, ++st) {
+          const uint32_t b = (uint32_t)(st & 1u);
+          if (!wait(a_full + b, (uint32_t)((st >> 1) & 1u))) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t k0 = c * KC, w = min(KC, Kp - k0), sbo_a = (w / 8) * 128u;
+          for (uint32_t ks = 0; ks < w / 16; ++ks) {
+            const uint32_t offa = ks * 256u, offb = (k0 / 16 + ks) * 256u;
+            uint64_t da[3], db[3];
+#pragma unroll
+            for (int part = 0; part < 3; ++part) {
+              da[part] = smem_desc(base + L.a[b][part] + offa, 128u, sbo_a);
+              db[part] = smem_desc(base + L.b[part] + offb, 128u, sbo_b);
+            }
+            const uint32_t acc0 = (c == 0 && ks == 0) ? 0u : 1u;
+            // the small cross products: x1y3 + x2y2 + x3y1 + x1y2 + x2y1
+            mma_bf16(acc_s, da[0], db[2], idesc, acc0);
+            mma_bf16(acc_s, da[1], db[1], idesc, 1u);
+            mma_bf16(acc_s, da[2], db[0], idesc, 1u);
+            mma_bf16(acc_s, da[0], db[1], idesc, 1u);
+            mma_bf16(acc_s, da[1], db[0], idesc, 1u);
+            mma_bf16(acc_b, da[0], db[0], idesc, acc0);  // x1y1
+          }
+          mma_commit(a_empty + b);  // the buffer is free once these complete
+          last_bar = a_empty + b;
+          last_par = (uint32_t)((st >> 1) & 1u);
+          if (c == nch - 1) mma_commit(acc_full + ab);
+        }
+      }
+      // every committed MMA completes before TMEM is freed
+      if (last_bar) (void)mbar_wait(last_bar, last_par, nullptr);
+    }
+  } else {
+    // ---- epilogue: warp quarter q reads TMEM lanes 32q.. (tile rows) ----------
+    const uint32_t q = (uint32_t)wid & 3u;
+    float pa[32], pb[32];
+    auto pivots = [&](uint64_t row0, uint32_t c0, float (&pv)[32]) {
+      const uint64_t gr = row0 + q * 32 + lane;
+      const bool rok = gr < rows;
+      const float* ap = Apiv + gr;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const uint32_t col = c0 + j;  // < Np <= 128: spoff / spiv cover it
+        const long long off = col < ncols ? spoff[col] : -1ll;
+        float a = 0.f;
+        if (off >= 0 && rok) {
+          a = ap[off];
+          if (spiv[col] < 0) a = -a;
+        }
+        pv[j] = a;
+      }
+    };
+    for (uint64_t i = 0; i < my_tiles; ++i) {
+      const uint64_t row0 = (blockIdx.x + i * gridDim.x) * kTpRows;
+      const uint64_t gr = row0 + q * 32 + lane;
+      const uint32_t ab = (uint32_t)(i & 1u);
+      pivots(row0, 0, pa);  // in flight while the MMAs finish
+      // lane 0 waits and the warp follows its answer (tcgen05.ld needs every lane)
+      const int ok = __shfl_sync(0xffffffffu,
+                                 lane == 0 ? (int)wait(acc_full + ab, (uint32_t)((i >> 1) & 1u))
+                                           : 0,
+                                 0);
+      if (!ok) break;
+      tc_fence_after();
+      const uint32_t t_s = tmem + 2u * ab * tmem_cols + ((q * 32u) << 16);
+      const uint32_t t_b = t_s + tmem_cols;
+      for (uint32_t g = 0; g < Np; g += 32) {
+        if (g + 32 < Np) pivots(row0, g + 32, pb);  // the next group's loads fly
+#pragma unroll
+        for (uint32_t u = 0; u < 32; u += 16) {
+          if (g + u < Np) {  // Np is a multiple of 32
+            float vs[16], vb[16];
+            tmem_ld16x2(t_s + g + u, t_b + g + u, vs, vb);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const uint32_t col = g + u + j;
+              if (gr < rows && col < ncols) {
+                const float val = (vs[j] + vb[j]) + pa[u + j];  // FP32, round to nearest
+                float* cp = C + (uint64_t)col * ldc + gr;
+                *cp = accumulate ? *cp + val : val;  // K chunks add in order
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) pa[j] = pb[j];
+      }
+      tc_fence_before();  // the TMEM reads before the accumulators are reused
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty + ab);
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (wid == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 ::"r"(tmem), "r"(4u * tmem_cols)
+                 : "memory");
+  }
+}
+
 }  // namespace
 
 bool gemm_tc_supported(uint32_t K, uint32_t ncols) {
-  if (K == 0 || ncols == 0 || K > 112 || ncols > 256) return false;
+  // one staging: the whole K (A tile and B in shared memory) and at most 128
+  // output columns (the epilogue's four 32-column quarters)
+  if (K == 0 || ncols == 0 || K > kTcChunkK || ncols > kTcChunkN) return false;
   const uint32_t Kp = (K + 15) & ~15u, Np = (ncols + 31) & ~31u;
   return TcLayout(Kp, Np).total <= 227 * 1024;
 }
@@ -433,16 +821,49 @@ static int launch_tc_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t
   return BGPU_OK;
 }
 
-// Subspaces larger than one staging (K > 112 or more than 128 output columns,
-// the 10M-cell solve's m = 200) run as K chunks of <= 112 and column chunks
-// of <= 128: each chunk's operands fit the 227 KB of shared memory, and the
-// K chunks of a column chunk add into C in chunk order (fixed, so the result
-// is the same on every run); the first K chunk adds the pivot columns.
+// The widest K chunk (a multiple of 16, at most 32) whose layout fits one
+// CTA's shared memory with B resident; 0 when none does.
+static uint32_t tp_chunk_k(uint32_t Kp, uint32_t Np) {
+  for (uint32_t kc = kTpMaxKc; kc >= 16; kc -= 16) {
+    const uint32_t k = std::min(kc, Kp);
+    if (TpLayout(Kp, Np, k).total <= kTpSmem) return k;
+  }
+  return 0;
+}
+
+static int launch_tp_chunk(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
+                           const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
+                           uint64_t ldc, int accumulate, const float* Apiv,
+                           const int* piv, int* err, cudaStream_t s) {
+  const uint32_t Kp = (K + 15) & ~15u, Np = (ncols + 31) & ~31u;
+  const uint32_t KC = tp_chunk_k(Kp, Np);
+  BGPU_REQUIRE(KC > 0 && ncols <= kTpChunkN, BGPU_ERR_UNSUPPORTED,
+               "tensor-core rotation: operands do not fit shared memory");
+  uint32_t tcols = 32;
+  while (tcols < Np) tcols <<= 1;
+  // at least 120 KB so that one CTA (and one TMEM allocation) runs per SM
+  const size_t smem = std::max<size_t>(TpLayout(Kp, Np, KC).total, 120 * 1024);
+  BGPU_CUDA(allow_max_smem(k_gemm_tc_pipe));
+  const uint64_t ntiles = (rows + kTpRows - 1) / kTpRows;
+  const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)num_sms());
+  k_gemm_tc_pipe<<<grid, kTpThreads, smem, s>>>(A, lda, rows, K, Bm, ldb, ncols, C, ldc,
+                                           Kp, Np, KC, tcols, accumulate, Apiv, piv, err);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+// One staging when the whole K and all output columns fit (K <= 112,
+// ncols <= 256: the 1M-cell solve's m = 100); otherwise the pipelined kernel,
+// output columns in chunks of <= 128 each reading all of K with B resident,
+// and a K that does not fit even with 16-wide A chunks (beyond ~230) as K
+// chunks of <= 128 added into C in chunk order (fixed, so the result is the
+// same on every run), the first adding the pivot columns. The pipelined
+// kernel stages A with cp.async: A's columns must start 16-byte aligned.
 int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                    const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
                    uint64_t ldc, float* dwork, int* piv, int* err, cudaStream_t s) {
   if (rows == 0 || ncols == 0) return BGPU_OK;
-  BGPU_REQUIRE(K >= 1 && ncols <= K && K <= kTcMaxK, BGPU_ERR_UNSUPPORTED,
+  BGPU_REQUIRE(K >= 1 && ncols <= K && K <= kTpMaxK, BGPU_ERR_UNSUPPORTED,
                "tensor-core rotation needs 1 <= ncols <= K <= 1024");
   BGPU_REQUIRE(dwork && piv, BGPU_ERR_INVALID, "tensor-core rotation needs its scratch");
   k_rot_pivots<<<(unsigned)ceil_div((uint64_t)ncols * 32, 256), 256, 0, s>>>(
@@ -450,11 +871,15 @@ int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
   BGPU_CHECK_LAUNCH();
   if (gemm_tc_supported(K, ncols))
     return launch_tc_chunk(A, lda, rows, K, dwork, K, ncols, C, ldc, 0, A, piv, err, s);
-  for (uint32_t n0 = 0; n0 < ncols; n0 += kTcChunkN) {
-    const uint32_t nc = std::min(kTcChunkN, ncols - n0);
-    for (uint32_t k0 = 0; k0 < K; k0 += kTcChunkK) {
-      const uint32_t kk = std::min(kTcChunkK, K - k0);
-      BGPU_TRY(launch_tc_chunk(A + (uint64_t)k0 * lda, lda, rows, kk,
+  BGPU_REQUIRE(((uintptr_t)A & 15u) == 0 && (lda & 3u) == 0, BGPU_ERR_UNSUPPORTED,
+               "tensor-core rotation needs 16-byte aligned columns of A when K > 112");
+  const uint32_t kchunk =
+      tp_chunk_k((K + 15) & ~15u, (std::min(ncols, kTpChunkN) + 31) & ~31u) ? K : 128u;
+  for (uint32_t n0 = 0; n0 < ncols; n0 += kTpChunkN) {
+    const uint32_t nc = std::min(kTpChunkN, ncols - n0);
+    for (uint32_t k0 = 0; k0 < K; k0 += kchunk) {
+      const uint32_t kk = std::min(kchunk, K - k0);
+      BGPU_TRY(launch_tp_chunk(A + (uint64_t)k0 * lda, lda, rows, kk,
                                dwork + (uint64_t)n0 * K + k0, K, nc,
                                C + (uint64_t)n0 * ldc, ldc, k0 > 0 ? 1 : 0, A,
                                k0 == 0 ? piv + n0 : nullptr, err, s));

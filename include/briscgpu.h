@@ -277,8 +277,9 @@ BGPU_API int bgpu_start_vector(uint64_t seed, uint32_t num_genes, float* out_hos
  * C rows x ncols (ldc). mode 1: FP32 SIMT; mode 2: tensor cores (tcgen05,
  * 3 x BF16 split operands, six cross products accumulated in FP32; a column
  * of Bm dominated by one entry (|entry| >= 1/2) is applied as that column of
- * A, added in FP32, plus the tensor-core product with the rest; K > 112 or
- * ncols > 128 run as chunks whose K parts add in a fixed order).
+ * A, added in FP32, plus the tensor-core product with the rest; ncols > 128
+ * runs as column chunks, K beyond ~230 as K chunks added in a fixed order;
+ * A's columns must start 16-byte aligned: A aligned, lda a multiple of 4).
  * Synchronous. */
 BGPU_API int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,
                                uint32_t K, const float* Bm, uint64_t ldb,
