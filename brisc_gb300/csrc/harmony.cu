@@ -37,9 +37,10 @@
 //    and sums them per cluster and batch; with the objective wanted, also
 //    the cells' k-means error and entropy terms (those of the final R with
 //    the Y of the pass: the objective after the pass);
-//  - writes its chunk's changes of E and O; the last CTA to finish (an atomic
-//    ticket after a fence, no waiting) adds every chunk's changes in chunk
-//    order to E and O, so the next block's launch sees them.
+//  - writes its chunk's changes of E and O; the last CTA of each group of 16
+//    chunks (an atomic ticket after a fence, no waiting) sums the group's in
+//    chunk order, and the last group adds the group sums to E and O in group
+//    order, so the next block's launch sees them.
 // R^T Z and the correction's R-weighted PC sums run as a register-tiled
 // SIMT reduction over cell ranges (k_h_rtm), its partials summed in range
 // order; the correction itself as a small GEMM per tile of one batch's cells
@@ -65,6 +66,7 @@ constexpr uint32_t kHMaxChunk = 1024;
 constexpr uint32_t kHCellsPerWarp = 4;       // cells a warp scores at once
 constexpr size_t kHSmemBudget = 110 * 1024;      // two block CTAs per SM
 constexpr size_t kHSmemBudgetOne = 220 * 1024;   // one block CTA per SM
+constexpr uint32_t kHFoldGroup = 16;  // chunks folded together before the final fold
 
 struct BlockArgs {
   const float* Z;
@@ -82,8 +84,10 @@ struct BlockArgs {
   float* R;                // n x C
   float* dE;               // chunks x B x C
   float* dO;
+  float* gE;               // fold groups x B x C: per-group sums of dE, dO
+  float* gO;
   double* obj;             // 2 per chunk (nullptr: objective not wanted)
-  uint32_t* ticket;
+  uint32_t* ticket;        // [0]: groups done; [1 + g]: chunks of group g done
   int init;                // initial assignments: no old sums, exp(tos (dot - 1))
 };
 
@@ -160,6 +164,32 @@ __device__ __forceinline__ void segment_sums(const float* rs, const uint32_t* se
     for (int u = 0; i < m; ++i, ++u) p[u] += col[(size_t)i * C];
     dst[b * C + j] += (p[0] + p[1]) + (p[2] + p[3]);
   }
+}
+
+// Column sums of two row-major arrays (rows of `stride` floats, `rows` rows,
+// read through L2: written by other CTAs): four interleaved partial sums per
+// column (rows 4i..4i+3 in order, the remainder into the first), combined in
+// a fixed order.
+__device__ __forceinline__ void sum_rows4(const float* a, const float* b, uint32_t rows,
+                                          uint32_t stride, float* sa, float* sb) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+  uint32_t k = 0;
+  for (; k + 4 <= rows; k += 4) {
+    a0 += __ldcg(a + (uint64_t)k * stride);
+    a1 += __ldcg(a + (uint64_t)(k + 1) * stride);
+    a2 += __ldcg(a + (uint64_t)(k + 2) * stride);
+    a3 += __ldcg(a + (uint64_t)(k + 3) * stride);
+    b0 += __ldcg(b + (uint64_t)k * stride);
+    b1 += __ldcg(b + (uint64_t)(k + 1) * stride);
+    b2 += __ldcg(b + (uint64_t)(k + 2) * stride);
+    b3 += __ldcg(b + (uint64_t)(k + 3) * stride);
+  }
+  for (; k < rows; ++k) {
+    a0 += __ldcg(a + (uint64_t)k * stride);
+    b0 += __ldcg(b + (uint64_t)k * stride);
+  }
+  *sa = (a0 + a1) + (a2 + a3);
+  *sb = (b0 + b1) + (b2 + b3);
 }
 
 template <int CPL>
@@ -405,30 +435,37 @@ __global__ void __launch_bounds__(kHThreads, 2) k_h_block(BlockArgs a) {
       a.obj[2 * blockIdx.x + 1] = y;
     }
   }
-  // the last CTA to finish folds every chunk's changes into E and O
+  // Fold every chunk's changes into E and O in two levels, with atomic
+  // tickets after fences (no waiting): the last CTA of each group of
+  // kHFoldGroup consecutive chunks sums the group's changes in chunk order;
+  // the last group to finish adds the group sums to E and O in group order.
   __threadfence();
   __syncthreads();
-  if (tid == 0) is_last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+  const uint32_t BC = B * C, nch = gridDim.x;
+  const uint32_t gi = blockIdx.x / kHFoldGroup, ngroups = (nch + kHFoldGroup - 1) / kHFoldGroup;
+  const uint32_t c0 = gi * kHFoldGroup, gsz = min(kHFoldGroup, nch - c0);
+  if (tid == 0) is_last = atomicAdd(a.ticket + 1 + gi, 1u) == gsz - 1;
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  const uint32_t BC = B * C, nch = gridDim.x;
   for (uint32_t t = tid; t < BC; t += kHThreads) {
-    float e[4] = {0.f, 0.f, 0.f, 0.f}, o[4] = {0.f, 0.f, 0.f, 0.f};
-    uint32_t c = 0;
-    for (; c + 4 <= nch; c += 4) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        e[u] += __ldcg(a.dE + (uint64_t)(c + u) * BC + t);
-        o[u] += __ldcg(a.dO + (uint64_t)(c + u) * BC + t);
-      }
-    }
-    for (int u = 0; c < nch; ++c, ++u) {
-      e[u] += __ldcg(a.dE + (uint64_t)c * BC + t);
-      o[u] += __ldcg(a.dO + (uint64_t)c * BC + t);
-    }
-    a.E[t] += (e[0] + e[1]) + (e[2] + e[3]);
-    a.O[t] += (o[0] + o[1]) + (o[2] + o[3]);
+    float e, o;
+    sum_rows4(a.dE + (uint64_t)c0 * BC + t, a.dO + (uint64_t)c0 * BC + t, gsz, BC, &e, &o);
+    a.gE[(uint64_t)gi * BC + t] = e;
+    a.gO[(uint64_t)gi * BC + t] = o;
+  }
+  if (tid == 0) a.ticket[1 + gi] = 0u;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) is_last = atomicAdd(a.ticket, 1u) == ngroups - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (uint32_t t = tid; t < BC; t += kHThreads) {
+    float e, o;
+    sum_rows4(a.gE + t, a.gO + t, ngroups, BC, &e, &o);
+    a.E[t] += e;
+    a.O[t] += o;
   }
   if (tid == 0) *a.ticket = 0u;
 }
@@ -755,8 +792,9 @@ int harmony_run(const float* PCs, float* Z, float* Y, float* R, const uint32_t* 
   const uint32_t npart = std::max(nr_nat, nr_b);
   const uint32_t nobj = std::max(nchunks, nblocks * max_cpb);
   const uint32_t max_launch_chunks = std::max(nchunks, max_cpb);
+  const uint32_t max_groups = (uint32_t)ceil_div(max_launch_chunks, kHFoldGroup);
 
-  float *E, *O, *Pr_d, *th_d, *dE, *dO, *part, *W;
+  float *E, *O, *Pr_d, *th_d, *dE, *dO, *gE, *gO, *part, *W;
   double* obj;
   uint32_t *order_d, *border_d, *ticket;
   uint64_t *starts_nat_d, *starts_b_d, *cor_tiles_d;
@@ -776,12 +814,14 @@ int harmony_run(const float* PCs, float* Z, float* Y, float* R, const uint32_t* 
     BGPU_TRY(dalloc(&th_d, B * 4ull));
     BGPU_TRY(dalloc(&dE, (uint64_t)max_launch_chunks * BC * 4));
     BGPU_TRY(dalloc(&dO, (uint64_t)max_launch_chunks * BC * 4));
+    BGPU_TRY(dalloc(&gE, (uint64_t)max_groups * BC * 4));
+    BGPU_TRY(dalloc(&gO, (uint64_t)max_groups * BC * 4));
     BGPU_TRY(dalloc(&part, (uint64_t)npart * C * d * 4));
     BGPU_TRY(dalloc(&W, (uint64_t)C * (B + 1) * d * 4));
     BGPU_TRY(dalloc(&obj, (uint64_t)nobj * 16));
     BGPU_TRY(dalloc(&order_d, n * 4));
     BGPU_TRY(dalloc(&border_d, n * 4));
-    BGPU_TRY(dalloc(&ticket, 16));
+    BGPU_TRY(dalloc(&ticket, (1ull + max_groups) * 4));
     BGPU_TRY(dalloc(&starts_nat_d, starts_nat.size() * 8));
     BGPU_TRY(dalloc(&starts_b_d, starts_b.size() * 8));
     BGPU_TRY(dalloc(&cor_tiles_d, cor_tiles.size() * 8));
@@ -798,7 +838,7 @@ int harmony_run(const float* PCs, float* Z, float* Y, float* R, const uint32_t* 
                               cudaMemcpyHostToDevice, s));
     BGPU_CUDA(cudaMemcpyAsync(starts_b_d, starts_b.data(), starts_b.size() * 8,
                               cudaMemcpyHostToDevice, s));
-    BGPU_CUDA(cudaMemsetAsync(ticket, 0, 16, s));
+    BGPU_CUDA(cudaMemsetAsync(ticket, 0, (1ull + max_groups) * 4, s));
     BGPU_CUDA(cudaMemsetAsync(E, 0, BC * 4ull, s));
     BGPU_CUDA(cudaMemsetAsync(O, 0, BC * 4ull, s));
     BGPU_CUDA(cudaMemsetAsync(obj, 0, (uint64_t)nobj * 16, s));
@@ -846,6 +886,8 @@ int harmony_run(const float* PCs, float* Z, float* Y, float* R, const uint32_t* 
     ba.R = R;
     ba.dE = dE;
     ba.dO = dO;
+    ba.gE = gE;
+    ba.gO = gO;
     ba.ticket = ticket;
     // initialisation over natural chunks, with the unnormalised Y
     ba.order = nullptr;
