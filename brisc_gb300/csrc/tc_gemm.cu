@@ -608,16 +608,18 @@ k_gemm_tc_pipe(const float* __restrict__ A, uint64_t lda, uint64_t rows, uint32_
     // end the loop are taken by thread 0 and shared through the producers'
     // barrier, so every producer thread reaches every barrier.
     __shared__ int pgo;
+    // a warp's 32 lanes take 32 consecutive rows of one k group: their reads
+    // of the ring ([k][row]) fall on 32 different banks
     const uint32_t wf = KC / 8, wl = (Kp - (nch - 1) * KC) / 8;
     uint32_t mf[kTpTasks], ml[kTpTasks];  // row | k group << 8 | 1 << 16 (0: none)
 #pragma unroll
     for (int i = 0; i < kTpTasks; ++i) {
       const uint32_t t = tid + i * kTpProducerThreads;
-      mf[i] = t < kTpRows * wf ? (((t >> 3) / wf) * 8 + (t & 7u)) | (((t >> 3) % wf) << 8) |
-                                     (1u << 16)
+      mf[i] = t < kTpRows * wf ? (((t >> 5) / wf) * 32 + (t & 31u)) |
+                                     (((t >> 5) % wf) << 8) | (1u << 16)
                                : 0u;
-      ml[i] = t < kTpRows * wl ? (((t >> 3) / wl) * 8 + (t & 7u)) | (((t >> 3) % wl) << 8) |
-                                     (1u << 16)
+      ml[i] = t < kTpRows * wl ? (((t >> 5) / wl) * 32 + (t & 31u)) |
+                                     (((t >> 5) % wl) << 8) | (1u << 16)
                                : 0u;
     }
     const uint64_t S = my_tiles * nch;
