@@ -106,7 +106,8 @@ def cythonize(reference: Path) -> None:
                              full_module_name="brisc." + src.stem)
         if res.num_errors:
             raise RuntimeError(f"cython failed on {src}")
-        print(f"cythonized {src.name} -> {out.relative_to(HERE)}")
+        # progress on stderr: stdout of a bench run is its one JSON line
+        print(f"cythonized {src.name} -> {out.relative_to(HERE)}", file=sys.stderr)
 
 
 def compile_all(jobs: int, modules: list[str] | None = None) -> Path:
@@ -145,7 +146,7 @@ def compile_all(jobs: int, modules: list[str] | None = None) -> Path:
 
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         for msg in ex.map(one, cpps):
-            print(msg)
+            print(msg, file=sys.stderr)
     stamp.write_text(" ".join(flags))
     return machine_dir()
 
