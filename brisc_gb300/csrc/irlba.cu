@@ -450,7 +450,7 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
                                 S.ub_last.as<double>(), S.sb64.as<double>(), S.tailw.p,
                                 S.mergew.p, S.oaw.as<double>(), S.svdwork.p,
                                 kRefineSteps, s));
-      S.launches += 7 + (m - kc > kMergeFp64TailMax ? 1 + 4 * kRefineSteps + 4 : 0);
+      S.launches += 7 + (m - kc > kMergeClosedTailMax ? 1 + 4 * kRefineSteps + 4 : 0);
       ++S.merged_svds;
     } else if (S.svd_mode == 1) {
       BGPU_TRY(launch_jacobi_svd(nullptr, S.B.as<double>(), m, S.Ub.as<float>(),

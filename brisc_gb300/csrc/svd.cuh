@@ -57,7 +57,7 @@ int launch_restart_check(const float* Ub, const float* Sb, const double* ub_last
 // mergew merge_work_bytes(m), refine_work svd_refine_doubles(m) doubles,
 // jacobi_gwork as for launch_jacobi_svd at size m (may be null where that
 // needs none).
-constexpr uint32_t kMergeFp64TailMax = 12;  // tails up to this size: FP64 Jacobi
+constexpr uint32_t kMergeClosedTailMax = 2;  // tails up to this size: closed form
 struct MergeWork {
   double *ds, *zs, *dn, *zn, *tau, *zhat, *lam, *rot_c, *rot_s, *znorm2;
   int *src, *defl, *ndpos, *defpos, *rot_p, *rot_q, *korig, *order, *state;

@@ -555,26 +555,21 @@ int launch_svd_merge(const double* B, uint32_t m, uint32_t kc, float* Ub, float*
   float* Sb_t = reinterpret_cast<float*>(take((size_t)m * 4));
   const MergeWork w = merge_work_carve(mergew, m);
 
-  // 1. the tail's SVD: FP64 Jacobi for a few rows, else the general FP32
-  //    Jacobi + FP64 Newton refinement at size t
-  const bool small = t <= kMergeFp64TailMax;
-  if (t <= 2) {
+  // 1. the tail's SVD: closed forms for one or two rows, else FP32 Jacobi +
+  //    FP64 Newton refinement at size t (an FP64 Jacobi of even a 3-12 row
+  //    tail takes longer on this GPU: its rotations are serial FP64 chains)
+  if (t <= kMergeClosedTailMax) {
     k_tail_small<<<1, 32, 0, s>>>(B, m, kc, Q64, sb_t);
     BGPU_CHECK_LAUNCH();
   } else {
     const unsigned tb = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(tt1, 256),
                                                                           1024));
-    k_build_tail<<<tb, 256, 0, s>>>(B, m, kc, L64, small ? nullptr : L32);
+    k_build_tail<<<tb, 256, 0, s>>>(B, m, kc, L64, L32);
     BGPU_CHECK_LAUNCH();
-    if (small) {
-      BGPU_TRY(launch_jacobi_svd(nullptr, L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t,
-                                 jacobi_gwork, nullptr, s, Q64));
-    } else {
-      BGPU_TRY(launch_jacobi_svd(L32, nullptr, t, Ub_t, Sb_t, Vbt_t, nullptr, nullptr,
-                                 jacobi_gwork, nullptr, s));
-      BGPU_TRY(launch_svd_refine(L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t, refine_work,
-                                 refine_steps, s, Q64));
-    }
+    BGPU_TRY(launch_jacobi_svd(L32, nullptr, t, Ub_t, Sb_t, Vbt_t, nullptr, nullptr,
+                               jacobi_gwork, nullptr, s));
+    BGPU_TRY(launch_svd_refine(L64, t, Ub_t, Sb_t, Vbt_t, ubl_t, sb_t, refine_work,
+                               refine_steps, s, Q64));
   }
   // 2. the merge
   k_merge_setup<<<1, 256, (size_t)4 * m * 8 + (size_t)2 * m * 4, s>>>(B, m, kc, Q64,
