@@ -119,3 +119,26 @@ def test_harmony_rejects_a_label_out_of_range(cuda, golden):
         H.harmony(PCs=c["PCs"], Z=c["PCs"].copy(), Y=c["Y_init"].copy(),
                   R=np.zeros((n, len(c["Y_init"])), np.float32),
                   batch_labels=c["batch_labels"], num_batches=2)
+
+
+@pytest.mark.parametrize("n,d,C,B,chunk", [(6000, 100, 200, 10, 256),  # 8 clusters a lane,
+                                           #  128-dim correction tiles, large tiles
+                                           (3000, 12, 20, 2, 64),      # one cluster a lane
+                                           (4000, 64, 64, 33, 300)])   # many batches
+def test_harmony_shapes_match_oracle(cuda, n, d, C, B, chunk):
+    """The kernel shapes the fixtures do not reach, against the oracle from
+    the same starting centroids: cluster counts above 128 and below 32, PCs
+    above 64, 33 batches (the block kernel's larger shared-memory tiles), a
+    chunk size that is not a power of two."""
+    from synth import batched_pcs
+    from oracle import harmony as oh
+    X, b = batched_pcs(n, d, 12, B, seed=n + C)
+    rng = np.random.default_rng(1)
+    Z0 = oh.normalize_rows(X)
+    Y0 = np.ascontiguousarray(Z0[rng.choice(n, C, replace=False)])
+    kw = dict(seed=2, chunk_size=chunk, max_iterations=4)
+    Zo, Ro = oh.harmony(X, Z0.copy(), Y0, b, B, **kw)
+    c = dict(PCs=X, batch_labels=b, num_batches=B, harmony_kwargs=kw, Y_init=Y0,
+             ref_Z=Zo, ref_R_head=Ro[:500])
+    Z, Y, R, it = _harmony(c)
+    check_against(c, Z, R[:500], **TOL)
