@@ -538,7 +538,9 @@ def run_batched(args):
     """Batched subset PCAs: one shared 3M x 2000 matrix partitioned into 64
     cell-type subsets (sizes log-uniform on [2k, 400k]); one 30-PC IRLBA per
     subset, each centred and scaled over its own cells. Sequential solves
-    (one at a time) against the batch (--concurrency solves in flight)."""
+    (one at a time) against the lock-step batch (every step kernel one launch
+    over all subsets), with independent solves on --concurrency streams
+    beside it."""
     import torch
     from brisc_gb300.batch import SharedMatrix, pca_subsets
     torch.cuda.init()
@@ -550,18 +552,38 @@ def run_batched(args):
     subsets = [np.sort(perm[bounds[i]:bounds[i + 1]]) for i in range(len(sizes))]
     S = SharedMatrix(C.indptr, C.indices, C.data, n, g, inv_size_factors=C.isf)
     for _ in range(max(args.warmup, 1)):  # warm the kernels on the smallest subsets
-        pca_subsets(S, sorted(subsets, key=len)[:4], num_PCs=k, concurrency=4)
+        pca_subsets(S, sorted(subsets, key=len)[:4], num_PCs=k, concurrency=4, mode="streams")
+        pca_subsets(S, sorted(subsets, key=len)[:4], num_PCs=k, concurrency=4, mode="fused")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    seq = pca_subsets(S, subsets, num_PCs=k, concurrency=1)
+    seq = pca_subsets(S, subsets, num_PCs=k, concurrency=1, mode="streams")
     t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    strm = pca_subsets(S, subsets, num_PCs=k, concurrency=args.concurrency, mode="streams")
+    t_strm = time.perf_counter() - t0
+    binfo = {}
     with Clocks(0) as clk:
         t0 = time.perf_counter()
-        bat = pca_subsets(S, subsets, num_PCs=k, concurrency=args.concurrency)
+        bat = pca_subsets(S, subsets, num_PCs=k, concurrency=args.concurrency, mode="fused",
+                          info=binfo)
         t_bat = time.perf_counter() - t0
-    same = all(np.array_equal(a.result.PCs, b.result.PCs) for a, b in zip(seq, bat))
+    same = all(np.array_equal(a.result.PCs, b.result.PCs) and
+               np.array_equal(a.result.PCs, c.result.PCs)
+               for a, b, c in zip(seq, bat, strm))
     from brisc_gb300.serve import percentile
     lat = [r.seconds for r in bat]
+
+    def solve_bytes(info: dict) -> float:
+        # algorithmic bytes of one solve: its products, Gram-Schmidt passes
+        # and restart rotations
+        return (info["lanczos_steps"] * info["matvec_bytes"]
+                + info["rmatvecs"] * info["rmatvec_bytes"]
+                + info["reorth_bytes"] + info["rotation_bytes"])
+    total_bytes = sum(solve_bytes(r.result.info) for r in bat)
+    launches = int(binfo["kernel_launches"])  # the fused batch's own launches
+    launches_seq = sum(int(r.result.info["kernel_launches"]) for r in seq)
+    steps = [int(r.result.info["lanczos_steps"]) for r in bat]
+    peak = measured_peaks()["hbm_gbs"]
     out = {"metric": "batched subset PCAs: solves/s (64 subsets of 3M x 2000, 30 PCs)",
            "value": len(subsets) / t_bat, "unit": "solves/s", "n_gpus": 1,
            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
@@ -569,14 +591,32 @@ def run_batched(args):
                                   f"{C.nnz:,} stored entries, {len(subsets)} subsets "
                                   f"of {sizes.min():,}-{sizes.max():,} cells, "
                                   f"{k} PCs, subspace {2 * k}",
-                      "concurrency": args.concurrency},
+                      "mode": "fused lock-step batch (one launch per step kernel "
+                              "over all subsets)",
+                      "layout_threads": args.concurrency},
            "sequential_solves_per_s": len(subsets) / t_seq,
            "vs_sequential": t_seq / t_bat,
            "batch_seconds": t_bat, "sequential_seconds": t_seq,
+           "layout_build_seconds": binfo.get("build_seconds"),
+           "streams": {"concurrency": args.concurrency, "seconds": t_strm,
+                       "solves_per_s": len(subsets) / t_strm,
+                       "vs_sequential": t_seq / t_strm},
            "bit_identical_to_sequential": same,
            "subset_seconds_p50": percentile(lat, 50),
            "subset_seconds_p99": percentile(lat, 99),
            "converged": int(sum(r.result.converged for r in bat)),
+           # the subsets partition the cells: a step of every subset reads each
+           # stored entry once, whether in one pass or in one pass per subset
+           "bytes": {"total_algorithmic": total_bytes,
+                     "per_solve_mean": total_bytes / len(bat),
+                     "batch_gbs": total_bytes / t_bat / 1e9,
+                     "batch_frac": total_bytes / t_bat / 1e9 / peak,
+                     "sequential_frac": total_bytes / t_seq / 1e9 / peak},
+           "kernel_launches": launches,
+           "kernel_launches_sequential": launches_seq,
+           "launches_per_s_batch": launches / t_bat,
+           "lanczos_steps": {"min": min(steps), "max": max(steps),
+                             "total": int(sum(steps))},
            "clocks": clk.summary()}
     print(json.dumps(out))
     return 0

@@ -40,6 +40,7 @@ class MatrixDesc(C.Structure):
         ("post_factors", C.c_void_p),
         ("panel_rows", C.c_uint32),
         ("kernels", C.c_uint32),
+        ("sell_panel_rows", C.c_uint32),
     ]
 
 
@@ -149,6 +150,8 @@ SIGNATURES = {
     "bgpu_solve_opts_default": (None, [C.POINTER(SolveOpts)]),
     "bgpu_irlba": (_i, [_vp, C.POINTER(SolveOpts), _vp, _i, _vp, _vp,
                         C.POINTER(SolveInfo), _vp]),
+    "bgpu_irlba_batch": (_i, [_vp, C.POINTER(SolveOpts), _u32, _vp, _i, _vp,
+                              C.POINTER(SolveInfo), C.POINTER(_u64), _vp]),
     "bgpu_irlba_f32": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i, _u64, _u32, _u32,
                             _u32, _f, _u32, _u64, _i, _i, _u32, _u64, _vp,
                             C.POINTER(_i)]),

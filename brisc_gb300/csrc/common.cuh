@@ -11,7 +11,11 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <mutex>
+#include <set>
 #include <string>
+#include <utility>
 
 #include "../../include/briscgpu.h"
 
@@ -62,13 +66,24 @@ int num_sms();                 // queried once per device
 // fixed value (rather than each launch's own size) means concurrent launches
 // from several threads never meet a limit another thread has just lowered.
 int device_smem_optin();
+// Set once per function and device (a launch path then pays no driver calls).
 template <typename F>
 inline cudaError_t allow_max_smem(F* fn) {
-  cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, fn);
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              device_smem_optin() - (int)a.sharedSizeBytes);
+  const auto key = std::make_pair((const void*)fn, dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count(key)) return cudaSuccess;
+  cudaFuncAttributes a;
+  e = cudaFuncGetAttributes(&a, fn);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           device_smem_optin() - (int)a.sharedSizeBytes);
+  if (e == cudaSuccess) done.insert(key);
+  return e;
 }
 
 __host__ __device__ inline uint64_t round_up(uint64_t x, uint64_t m) {
@@ -126,9 +141,10 @@ __device__ __forceinline__ uint2 ld_stream_u2(const void* p) {
 
 // Normalised value of one raw count in the fused layout: the reference's
 // `log1p(data[j] * inverse_size_factor)` (brisc/normalize.pyx:81), evaluated
-// in float exactly as written there.
+// in float exactly as written there (the product rounded before the log, in
+// every kernel that inlines this).
 __device__ __forceinline__ float norm_count(uint32_t count, float isf) {
-  return log1pf((float)count * isf);
+  return log1pf(__fmul_rn((float)count, isf));
 }
 
 }  // namespace bgpu

@@ -19,8 +19,16 @@ namespace bgpu {
 
 namespace {
 
+// The kernel bodies below are shared by a single-solve kernel and its
+// multi-task form (multi.cuh). Their products and sums are written with
+// explicit rounding intrinsics: the compiler may not fuse a multiply and an
+// add one way in one kernel and another way in the other, so both compute
+// the same bits.
 __device__ __forceinline__ float dot4(float4 a, float4 b) {
-  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+  return __fmaf_rn(a.w, b.w, __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x))));
+}
+__device__ __forceinline__ float sumsq4(float a, float b, float c, float d) {
+  return __fmaf_rn(d, d, __fmaf_rn(c, c, __fmaf_rn(b, b, __fmul_rn(a, a))));
 }
 
 // Adaptive second Gram-Schmidt pass: gate = {|y1|^2, |y0 - mean|^2} of the
@@ -40,15 +48,15 @@ __device__ __forceinline__ bool second_pass_skipped(const float* gate) {
 // with kDotCols 16-byte loads in flight).
 constexpr int kDotCols = 4;
 
-__global__ void __launch_bounds__(256, 8)
-k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
-        const float* __restrict__ y, float* __restrict__ part,
-        uint32_t pstride, int with_sum, const float* __restrict__ gate) {
+__device__ __forceinline__ void udots_body(const float* __restrict__ U, uint64_t ldu,
+                                           uint32_t ncols, const float* __restrict__ y,
+                                           float* __restrict__ part, uint32_t pstride,
+                                           int with_sum, const float* __restrict__ gate,
+                                           uint64_t b) {
   if (second_pass_skipped(gate)) return;
   extern __shared__ float wsum[];  // 8 x (ncols + 1)
   const uint32_t ld = ncols + 1;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint64_t b = blockIdx.x;
   const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
   const bool in = row0 < ldu;
   const float4 yv = in ? *reinterpret_cast<const float4*>(y + row0)
@@ -84,6 +92,21 @@ k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
     for (int w = 0; w < 8; ++w) t += wsum[w * ld + c];
     part[b * pstride + c] = t;
   }
+}
+
+__global__ void __launch_bounds__(256, 8)
+k_udots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+        const float* __restrict__ y, float* __restrict__ part,
+        uint32_t pstride, int with_sum, const float* __restrict__ gate) {
+  udots_body(U, ldu, ncols, y, part, pstride, with_sum, gate, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256, 8)
+k_udots_multi(const __grid_constant__ TaskList<UdotsTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const UdotsTask& t = L.t[i];
+  udots_body(t.U, t.ldu, t.ncols, t.y, t.part, t.pstride, t.with_sum, t.gate,
+             blockIdx.x - L.first[i]);
 }
 
 // alpha = max(sqrt(sum_b part[b * pstride]), 1e-8) in FP64 (clip_val,
@@ -127,15 +150,17 @@ __device__ void finish_norm_block(const float* part, uint64_t nblocks,
   }
 }
 
-__global__ void __launch_bounds__(256, 8)  // one wave, as k_udots
-k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
-          const float* __restrict__ coef, const float* __restrict__ mean_sum,
-          uint64_t n, const float* y_in, float* y_out,  // may be the same
-          float* __restrict__ norm_part, uint32_t pstride, int with_centred,
-          const float* __restrict__ gate, unsigned long long* __restrict__ taken,
-          NormFinish fin) {
+// b: the block; nblocks: the blocks of the launch (the last to finish
+// finishes the norm)
+__device__ __forceinline__ void uupdate_body(
+    const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+    const float* __restrict__ coef, const float* __restrict__ mean_sum, uint64_t n,
+    const float* y_in, float* y_out,  // may be the same
+    float* __restrict__ norm_part, uint32_t pstride, int with_centred,
+    const float* __restrict__ gate, unsigned long long* __restrict__ taken,
+    const NormFinish& fin, uint64_t b, uint32_t nblocks) {
   if (second_pass_skipped(gate)) return;
-  if (taken && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (taken && b == 0 && threadIdx.x == 0) {
     taken[0] += 1ull;
     taken[1] += ncols;
   }
@@ -143,7 +168,6 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
   __shared__ float red[2][8];
   for (uint32_t c = threadIdx.x; c < ncols; c += blockDim.x) cs[c] = coef[c];
   __syncthreads();
-  const uint64_t b = blockIdx.x;
   const uint64_t row0 = b * kRowBlock + threadIdx.x * 4ull;
   float sq = 0.f, sqc = 0.f;
   if (row0 < ldu) {
@@ -154,24 +178,24 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
       const float cy = (row0 + 1 < n) ? yv.y - mean : 0.f;
       const float cz = (row0 + 2 < n) ? yv.z - mean : 0.f;
       const float cw = (row0 + 3 < n) ? yv.w - mean : 0.f;
-      sqc = cx * cx + cy * cy + cz * cz + cw * cw;
+      sqc = sumsq4(cx, cy, cz, cw);
     }
     float4 t = make_float4(mean, mean, mean, mean);
 #pragma unroll 4
     for (uint32_t c = 0; c < ncols; ++c) {
       const float4 u = __ldcs(reinterpret_cast<const float4*>(U + c * ldu + row0));
       const float w = cs[c];
-      t.x += u.x * w;
-      t.y += u.y * w;
-      t.z += u.z * w;
-      t.w += u.w * w;
+      t.x = __fmaf_rn(u.x, w, t.x);
+      t.y = __fmaf_rn(u.y, w, t.y);
+      t.z = __fmaf_rn(u.z, w, t.z);
+      t.w = __fmaf_rn(u.w, w, t.w);
     }
     yv.x = (row0 + 0 < n) ? yv.x - t.x : 0.f;
     yv.y = (row0 + 1 < n) ? yv.y - t.y : 0.f;
     yv.z = (row0 + 2 < n) ? yv.z - t.z : 0.f;
     yv.w = (row0 + 3 < n) ? yv.w - t.w : 0.f;
     *reinterpret_cast<float4*>(y_out + row0) = yv;
-    sq = yv.x * yv.x + yv.y * yv.y + yv.z * yv.z + yv.w * yv.w;
+    sq = sumsq4(yv.x, yv.y, yv.z, yv.w);
   }
   if (norm_part) {
     sq = warp_sum(sq);
@@ -193,13 +217,33 @@ k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
       __shared__ bool last;
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) last = atomicAdd(fin.counter, 1u) == gridDim.x - 1;
+      if (threadIdx.x == 0) last = atomicAdd(fin.counter, 1u) == nblocks - 1;
       __syncthreads();
       if (!last) return;
       __threadfence();
-      finish_norm_block(norm_part, gridDim.x, pstride, with_centred, fin);
+      finish_norm_block(norm_part, nblocks, pstride, with_centred, fin);
     }
   }
+}
+
+__global__ void __launch_bounds__(256, 8)  // one wave, as k_udots
+k_uupdate(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
+          const float* __restrict__ coef, const float* __restrict__ mean_sum,
+          uint64_t n, const float* y_in, float* y_out,  // may be the same
+          float* __restrict__ norm_part, uint32_t pstride, int with_centred,
+          const float* __restrict__ gate, unsigned long long* __restrict__ taken,
+          NormFinish fin) {
+  uupdate_body(U, ldu, ncols, coef, mean_sum, n, y_in, y_out, norm_part, pstride,
+               with_centred, gate, taken, fin, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(256, 8)
+k_uupdate_multi(const __grid_constant__ TaskList<UupdateTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const UupdateTask& t = L.t[i];
+  uupdate_body(t.U, t.ldu, t.ncols, t.coef, t.mean_sum, t.n, t.y_in, t.y_out,
+               t.norm_part, t.pstride, t.with_centred, t.gate, t.taken, t.fin,
+               blockIdx.x - L.first[i], L.first[i + 1] - L.first[i]);
 }
 
 // CGS2 middle pass, fused: for one 256-row block, y1 = y0 - (mean + U c1)
@@ -263,13 +307,15 @@ k_uupdate_dots(const float* __restrict__ U, uint64_t ldu, uint32_t ncols,
 // (lane = column, so every load is one coalesced 128-byte row run); its 32
 // warps take blocks b = w, w + 32, ... and the 32 warp sums are added in warp
 // order, a fixed order whatever the timing.
-__global__ void __launch_bounds__(1024)
-k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
-              uint32_t ncols, float* __restrict__ out, const float* __restrict__ gate) {
+__device__ __forceinline__ void reduce_cols_body(const float* __restrict__ part,
+                                                 uint64_t nblocks, uint32_t pstride,
+                                                 uint32_t ncols, float* __restrict__ out,
+                                                 const float* __restrict__ gate,
+                                                 uint32_t b) {
   if (second_pass_skipped(gate)) return;
   __shared__ float ws[32][33];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t c = blockIdx.x * 32 + lane;
+  const uint32_t c = b * 32 + lane;
   float t = 0.f;
   if (c < ncols) {
     // eight loads in flight, added in block order
@@ -290,6 +336,20 @@ k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride
     for (int w = 0; w < 32; ++w) r += ws[w][lane];
     out[c] = r;
   }
+}
+
+__global__ void __launch_bounds__(1024)
+k_reduce_cols(const float* __restrict__ part, uint64_t nblocks, uint32_t pstride,
+              uint32_t ncols, float* __restrict__ out, const float* __restrict__ gate) {
+  reduce_cols_body(part, nblocks, pstride, ncols, out, gate, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(1024)
+k_reduce_cols_multi(const __grid_constant__ TaskList<ReduceColsTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const ReduceColsTask& t = L.t[i];
+  reduce_cols_body(t.part, t.nblocks, t.pstride, t.ncols, t.out, t.gate,
+                   blockIdx.x - L.first[i]);
 }
 
 __global__ void __launch_bounds__(1024)
@@ -347,13 +407,14 @@ k_vstep(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
 // memory, every CTA summing the 8 partials in rank order (so all CTAs hold
 // the same bits and the result does not depend on timing).
 constexpr int kVCluster = 8;
+static_assert(kVCluster == (int)kVStepCtas, "one V-step task is one cluster");
 constexpr int kVThreads = 1024;
 constexpr int kVSplit = 4;  // threads sharing one gene's update sum
 
-__global__ void __cluster_dims__(kVCluster, 1, 1) __launch_bounds__(kVThreads)
-k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
-                uint32_t g, uint32_t j, uint32_t m, const float* __restrict__ scal,
-                double* __restrict__ B, float* __restrict__ rem, int passes) {
+__device__ __forceinline__ void vstep_cluster_body(
+    const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv, uint32_t g,
+    uint32_t j, uint32_t m, const float* __restrict__ scal, double* __restrict__ B,
+    float* __restrict__ rem, int passes) {
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) float vsm[];
   const uint32_t slice = (g + kVCluster - 1) / kVCluster;
@@ -375,7 +436,7 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
   const float alpha = scal[0];
   const float* vj = V + (uint64_t)j * ldv;
   for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
-    zs[c - c0] = zin[c] - alpha * vj[c];  // pca.pyx:1104-1105
+    zs[c - c0] = __fmaf_rn(-alpha, vj[c], zin[c]);  // pca.pyx:1104-1105
   __syncthreads();
   for (int pass = 0; pass < npass; ++pass) {
     float* pdp = pd + (pass & 1) * (m + 1);
@@ -385,9 +446,9 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
       float d = 0.f;
       if (col <= j) {
         const float* vc = V + (uint64_t)col * ldv;
-        for (uint32_t c = c0 + lane; c < c1; c += 32) d += vc[c] * zs[c - c0];
+        for (uint32_t c = c0 + lane; c < c1; c += 32) d = __fmaf_rn(vc[c], zs[c - c0], d);
       } else {
-        for (uint32_t c = c0 + lane; c < c1; c += 32) d += zs[c - c0] * zs[c - c0];
+        for (uint32_t c = c0 + lane; c < c1; c += 32) d = __fmaf_rn(zs[c - c0], zs[c - c0], d);
       }
       d = warp_sum(d);
       if (lane == 0) pdp[col] = d;
@@ -406,7 +467,7 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
       float acc = 0.f;
       if (c < c1)
         for (uint32_t col = h; col <= j; col += kVSplit)
-          acc += V[c + (uint64_t)col * ldv] * dots[col];
+          acc = __fmaf_rn(V[c + (uint64_t)col * ldv], dots[col], acc);
       upd[t] = acc;
     }
     __syncthreads();
@@ -421,7 +482,7 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
     if (adaptive && pass == 0) {
       float s1 = 0.f;
       for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
-        s1 += zs[c - c0] * zs[c - c0];
+        s1 = __fmaf_rn(zs[c - c0], zs[c - c0], s1);
       s1 = warp_sum(s1);
       if (lane == 0) wz[wid] = s1;
       __syncthreads();
@@ -440,7 +501,7 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
   if (j + 1 < m) {
     double ss = 0.0;
     for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads)
-      ss += (double)zs[c - c0] * zs[c - c0];
+      ss = __fma_rn((double)zs[c - c0], (double)zs[c - c0], ss);
     ss = warp_sum(ss);
     if (lane == 0) wred[wid] = ss;
     __syncthreads();
@@ -461,6 +522,20 @@ k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t l
     for (uint32_t c = c0 + threadIdx.x; c < c1; c += kVThreads) out[c] = zs[c - c0];
   }
   cluster.sync();  // no CTA leaves while another may read its shared memory
+}
+
+__global__ void __cluster_dims__(kVCluster, 1, 1) __launch_bounds__(kVThreads)
+k_vstep_cluster(const float* __restrict__ zin, float* __restrict__ V, uint64_t ldv,
+                uint32_t g, uint32_t j, uint32_t m, const float* __restrict__ scal,
+                double* __restrict__ B, float* __restrict__ rem, int passes) {
+  vstep_cluster_body(zin, V, ldv, g, j, m, scal, B, rem, passes);
+}
+
+// one cluster per task: CTAs [8 i, 8 i + 8) of the grid
+__global__ void __cluster_dims__(kVCluster, 1, 1) __launch_bounds__(kVThreads)
+k_vstep_cluster_multi(const __grid_constant__ TaskList<VstepTask> L) {
+  const VstepTask& t = L.t[blockIdx.x / kVCluster];
+  vstep_cluster_body(t.z, t.V, t.ldv, t.g, t.j, t.m, t.scal, t.B, t.rem, t.passes);
 }
 
 // Tall-skinny SIMT GEMM: CTA tile 128 rows x 128 columns, K in steps of 16.
@@ -615,12 +690,20 @@ int launch_reduce_cols(const float* part, uint64_t nblocks, uint32_t pstride,
   return BGPU_OK;
 }
 
+static size_t vstep_cluster_smem(uint32_t g, uint32_t m) {
+  const uint32_t slice = (g + kVCluster - 1) / kVCluster;
+  return ((size_t)((slice + 3) & ~3u) + 2ull * (m + 1) + ((m + 4) & ~3u) +
+          (size_t)kVSplit * slice) * sizeof(float);
+}
+
+bool vstep_cluster_fits(uint32_t g, uint32_t m) {
+  return vstep_cluster_smem(g, m) <= 48 * 1024;
+}
+
 int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
                  uint32_t j, uint32_t m, const float* scal, double* B,
                  float* rem, int passes, cudaStream_t s) {
-  const uint32_t slice = (g + kVCluster - 1) / kVCluster;
-  const size_t csm = ((size_t)((slice + 3) & ~3u) + 2ull * (m + 1) +
-                      ((m + 4) & ~3u) + (size_t)kVSplit * slice) * sizeof(float);
+  const size_t csm = vstep_cluster_smem(g, m);
   if (csm <= 48 * 1024) {
     k_vstep_cluster<<<kVCluster, kVThreads, csm, s>>>(z, V, ldv, g, j, m, scal, B,
                                                      rem, passes);
@@ -628,6 +711,53 @@ int launch_vstep(const float* z, float* V, uint64_t ldv, uint32_t g,
     k_vstep<<<1, 1024, (size_t)m * sizeof(float), s>>>(  // adaptive: 2 passes
         z, V, ldv, g, j, m, scal, B, rem, passes == 0 ? 2 : passes);
   }
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_udots_multi(const TaskList<UdotsTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  uint32_t nc = 0;
+  for (uint32_t i = 0; i < L.count; ++i) nc = std::max(nc, L.t[i].ncols);
+  const size_t smem = 8ull * (nc + 1) * sizeof(float);
+  BGPU_REQUIRE(smem <= 227 * 1024, BGPU_ERR_UNSUPPORTED, "U dots: too many columns");
+  if (smem > 48 * 1024) BGPU_CUDA(allow_max_smem(k_udots_multi));
+  k_udots_multi<<<L.grid(), 256, smem, s>>>(L);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_reduce_cols_multi(const TaskList<ReduceColsTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  k_reduce_cols_multi<<<L.grid(), 1024, 0, s>>>(L);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_uupdate_multi(const TaskList<UupdateTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  uint32_t nc = 1;
+  for (uint32_t i = 0; i < L.count; ++i) {
+    const UupdateTask& t = L.t[i];
+    BGPU_REQUIRE(!t.fin.B || (t.norm_part && t.fin.counter && t.fin.scal), BGPU_ERR_INVALID,
+                 "U update: norm finish needs partials, a ticket counter and scal");
+    nc = std::max(nc, t.ncols);
+  }
+  k_uupdate_multi<<<L.grid(), 256, (size_t)nc * 4, s>>>(L);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_vstep_multi(const TaskList<VstepTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  size_t csm = 0;
+  for (uint32_t i = 0; i < L.count; ++i) {
+    BGPU_REQUIRE(L.first[i + 1] - L.first[i] == kVStepCtas &&
+                     vstep_cluster_fits(L.t[i].g, L.t[i].m),
+                 BGPU_ERR_INVALID, "V step: a task is one cluster of kVStepCtas CTAs");
+    csm = std::max(csm, vstep_cluster_smem(L.t[i].g, L.t[i].m));
+  }
+  k_vstep_cluster_multi<<<L.grid(), kVThreads, csm, s>>>(L);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "multi.cuh"
 
 namespace bgpu {
 
@@ -88,6 +89,61 @@ bool gemm_tc_supported(uint32_t K, uint32_t ncols);
 int launch_gemm_tc(const float* A, uint64_t lda, uint64_t rows, uint32_t K,
                    const float* Bm, uint64_t ldb, uint32_t ncols, float* C,
                    uint64_t ldc, float* dwork, int* piv, int* err, cudaStream_t s);
+
+// Fused multi-solve forms of the step kernels (multi.cuh): one launch over
+// every task, each task's CTAs computing what the single launch above
+// computes for its arguments. CTAs per task (the caller adds them with
+// TaskList::add): udots and uupdate `nblocks` (the single launch's grid),
+// reduce_cols ceil(ncols / 32) (tasks with ncols == 0 are left out), vstep
+// kVStepCtas (one thread-block cluster).
+struct UdotsTask {
+  const float* U;
+  uint64_t ldu;
+  const float* y;
+  float* part;
+  const float* gate;
+  uint32_t ncols, pstride;
+  int with_sum;
+};
+struct ReduceColsTask {
+  const float* part;
+  uint64_t nblocks;
+  float* out;
+  const float* gate;
+  uint32_t pstride, ncols;
+};
+struct UupdateTask {
+  const float* U;
+  uint64_t ldu;
+  const float* coef;
+  const float* mean_sum;
+  uint64_t n;
+  const float* y_in;
+  float* y_out;
+  float* norm_part;
+  const float* gate;
+  unsigned long long* taken;
+  NormFinish fin;
+  uint32_t ncols, pstride;
+  int with_centred;
+};
+struct VstepTask {
+  const float* z;
+  float* V;
+  uint64_t ldv;
+  const float* scal;
+  double* B;
+  float* rem;
+  uint32_t g, j, m;
+  int passes;
+};
+constexpr uint32_t kVStepCtas = 8;
+// whether launch_vstep runs (g, m) on one cluster (the multi form's only path)
+bool vstep_cluster_fits(uint32_t g, uint32_t m);
+int launch_udots_multi(const TaskList<UdotsTask>& L, cudaStream_t s);
+int launch_reduce_cols_multi(const TaskList<ReduceColsTask>& L, cudaStream_t s);
+int launch_uupdate_multi(const TaskList<UupdateTask>& L, cudaStream_t s);
+int launch_vstep_multi(const TaskList<VstepTask>& L, cudaStream_t s);
 
 // B (m x (m+1), column-major FP64) -> float copy for the small SVD.
 int launch_b_to_float(const double* B, uint32_t m, float* Bf, cudaStream_t s);

@@ -11,11 +11,13 @@
 // by Ub again (pca.pyx:1210-1215 then 1253), mixing in stale buffer columns;
 // here the last restart is not rotated, so the returned PCs are the Ritz
 // vectors of the final SVD, scaled by their singular values.
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -109,7 +111,11 @@ struct Buf {
   cudaStream_t s = nullptr;
   Buf() = default;
   Buf(const Buf&) = delete;
-  ~Buf() { if (p) cudaFreeAsync(p, s); }
+  ~Buf() { reset(); }
+  void reset() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+  }
   template <typename T>
   T* as() const { return (T*)p; }
 };
@@ -127,6 +133,8 @@ int balloc(Buf& b, size_t bytes, bool zero, cudaStream_t s) {
   if (zero) BGPU_CUDA(cudaMemsetAsync(b.p, 0, bytes, s));
   return BGPU_OK;
 }
+
+constexpr int kRefineSteps = 3;  // Newton steps after the FP32 Jacobi
 
 struct HostStatus {
   RestartStatus v{};
@@ -264,7 +272,9 @@ struct Solver {
   float* Ucol(uint32_t j) const { return U.as<float>() + (uint64_t)j * ldu; }
   float* Vcol(uint32_t j) const { return V.as<float>() + (uint64_t)j * ldv; }
 
-  int step(uint32_t j) {
+  // One Lanczos step on stream `s` (the solve's own stream, or the stream
+  // of a batch that launches this solve's kernels on it).
+  int step(uint32_t j, cudaStream_t s) {
     float* y0p = y0.as<float>();
     float* y1p = y1.as<float>();
     float* partp = part.as<float>();
@@ -374,16 +384,108 @@ struct Solver {
     launches += 2;  // reduce_panels_t, vstep
     return BGPU_OK;
   }
+
+  // Gene scaling (pca.pyx:790-799), start vector (pca.pyx:801-806) and the
+  // first smax (pca.pyx:688). Synchronises: v0 and smax0 are host values.
+  int begin(uint64_t seed) {
+    BGPU_TRY(launch_gene_stddev(X, sdpart.as<double>(), sd.as<float>(), s));
+    launches += 2;
+    std::vector<float> v0(g);
+    start_vector(seed, g, v0.data());
+    BGPU_CUDA(cudaMemcpyAsync(Vcol(0), v0.data(), g * 4, cudaMemcpyHostToDevice, s));
+    const float smax0 = 2.4221817809573368e-05f;  // pca.pyx:688
+    BGPU_CUDA(cudaMemcpyAsync(smax.p, &smax0, 4, cudaMemcpyHostToDevice, s));
+    BGPU_CUDA(cudaStreamSynchronize(s));
+    return BGPU_OK;
+  }
+
+  // The restart's small SVD of B (pca.pyx:1178) after a cycle that started
+  // at column kc.
+  int restart_svd(uint32_t kc) {
+    BGPU_TRY(ev_begin(2));
+    if (svd_mode == 0 && kc >= 1) {
+      // B = restart arrow + the cycle's Lanczos rows: the tail's SVD (t = m -
+      // kc rows) and an FP64 secular-equation merge instead of a full SVD
+      BGPU_TRY(launch_svd_merge(B.as<double>(), m, kc, Ub.as<float>(), Sb.as<float>(),
+                                Vbt.as<float>(), ub_last.as<double>(), sb64.as<double>(),
+                                tailw.p, mergew.p, oaw.as<double>(), svdwork.p,
+                                kRefineSteps, s));
+      launches += 7 + (m - kc > kMergeClosedTailMax ? 1 + 4 * kRefineSteps + 4 : 0);
+      ++merged_svds;
+    } else if (svd_mode == 1) {
+      BGPU_TRY(launch_jacobi_svd(nullptr, B.as<double>(), m, Ub.as<float>(), Sb.as<float>(),
+                                 Vbt.as<float>(), ub_last.as<double>(), sb64.as<double>(),
+                                 svdwork.p, svdinfo.as<int>(), s));
+      launches += 2;
+    } else {
+      BGPU_TRY(launch_b_to_float(B.as<double>(), m, Bf.as<float>(), s));
+      BGPU_TRY(launch_jacobi_svd(Bf.as<float>(), nullptr, m, Ub.as<float>(), Sb.as<float>(),
+                                 Vbt.as<float>(), nullptr, nullptr, svdwork.p,
+                                 svdinfo.as<int>(), s));
+      // FP64 Newton refinement of the FP32 factors: three quadratically
+      // convergent steps separate the vectors of close singular values (the
+      // Jacobi leaves pairs 6e-5 apart mixed by ~2 %), so the convergence test
+      // reads FP64-accurate last entries of Ub, as with an FP64 SVD
+      BGPU_TRY(launch_svd_refine(B.as<double>(), m, Ub.as<float>(), Sb.as<float>(),
+                                 Vbt.as<float>(), ub_last.as<double>(), sb64.as<double>(),
+                                 oaw.as<double>(), kRefineSteps, s));
+      launches += 2 + 1 + 4 * kRefineSteps + 4;
+    }
+    BGPU_TRY(ev_end());
+    return BGPU_OK;
+  }
+
+  // Convergence test and next k_current (pca.pyx:1180-1209) into st, then
+  // st and the device error word copied to host_st / host_err (pinned
+  // memory for a copy that does not block the host).
+  int restart_check(uint32_t kc, RestartStatus* host_st, int* host_err) {
+    BGPU_TRY(launch_restart_check(Ub.as<float>(), Sb.as<float>(), ub_last.as<double>(),
+                                  sb64.as<double>(), m, k, rem.as<float>(), g, tol,
+                                  smax.as<float>(), kc, B.as<double>(),
+                                  st.as<RestartStatus>(),
+                                  trace ? ratios.as<float>() : nullptr, s));
+    // restart status and the device error word in one stream round trip (no
+    // legacy-stream copies: those could wait on other streams' work)
+    BGPU_CUDA(cudaMemcpyAsync(host_st, st.p, sizeof(RestartStatus), cudaMemcpyDeviceToHost,
+                              s));
+    BGPU_CUDA(cudaMemcpyAsync(host_err, derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return BGPU_OK;
+  }
+
+  // Restart rotation (pca.pyx:1210-1226): U <- U Ub[:, :kc], V <- V Vbt^T,
+  // V[:, kc] = the remainder.
+  int rotate(uint32_t kc) {
+    BGPU_TRY(ev_begin(5));
+    if (rot_mode == 2)
+      BGPU_TRY(launch_gemm_tc(U.as<float>(), ldu, n, m, Ub.as<float>(), m, kc,
+                              Unew.as<float>(), ldu, rotd.as<float>(), rotpiv.as<int>(),
+                              derr.as<int>(), s));
+    else
+      BGPU_TRY(launch_gemm_ts(U.as<float>(), ldu, n, m, Ub.as<float>(), 1, m, nullptr, kc,
+                              Unew.as<float>(), ldu, false, s));
+    BGPU_TRY(launch_gemm_ts(V.as<float>(), ldv, g, m, Vbt.as<float>(), m, 1, nullptr, kc,
+                            Vnew.as<float>(), ldv, false, s));
+    BGPU_CUDA(cudaMemcpyAsync(Vnew.as<float>() + (uint64_t)kc * ldv, rem.p, g * 4,
+                              cudaMemcpyDeviceToDevice, s));
+    BGPU_TRY(ev_end());
+    std::swap(U.p, Unew.p);
+    std::swap(V.p, Vnew.p);
+    launches += 2;
+    rotation_bytes += ((double)n + g) * ((double)m + kc) * 4.0;
+    return BGPU_OK;
+  }
+
+  // Final PCs (pca.pyx:1239-1255): pout = U . (Ub[:, :k] * Sb[:k]), C order.
+  int final_pcs(float* pout) {
+    BGPU_TRY(launch_gemm_ts(U.as<float>(), ldu, n, m, Ub.as<float>(), 1, m, Sb.as<float>(),
+                            k, pout, k, true, s));
+    launches += 1;
+    return BGPU_OK;
+  }
 };
 
-}  // namespace
-
-constexpr int kRefineSteps = 3;  // Newton steps after the FP32 Jacobi
-
-int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
-                int pcs_on_device, float* svals, float* loadings,
-                bgpu_solve_info* info, cudaStream_t s) {
-  const auto t0 = std::chrono::steady_clock::now();
+// Settings shared by the single and the batched drivers.
+int check_opts(const Matrix& X, const bgpu_solve_opts& o) {
   BGPU_REQUIRE(o.k >= 1, BGPU_ERR_INVALID, "num_PCs (k) must be >= 1");
   BGPU_REQUIRE(o.subspace_size >= o.k, BGPU_ERR_INVALID,
                "subspace_size must be >= num_PCs");
@@ -397,35 +499,36 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
   BGPU_REQUIRE(o.max_iterations >= 1, BGPU_ERR_INVALID,
                "max_iterations must be >= 1");
   BGPU_REQUIRE(o.tolerance > 0.f, BGPU_ERR_INVALID, "tolerance must be > 0");
+  BGPU_REQUIRE(o.svd_mode <= 2, BGPU_ERR_INVALID, "svd_mode must be 0, 1 or 2");
+  BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
+  return BGPU_OK;
+}
+
+void configure(Solver& S, const bgpu_solve_opts& o) {
+  S.profile = o.profile != 0;
+  S.svd_mode = o.svd_mode;
+  S.svd64 = o.svd_mode == 1;
+  // subspaces beyond one shared-memory staging run as K / column chunks
+  const bool tc_ok = o.subspace_size <= 1024;
+  S.rot_mode = o.rotation_mode == 0 ? (tc_ok ? 2 : 1) : (int)o.rotation_mode;
+  const char* et = std::getenv("BGPU_TRACE");
+  S.trace = et && et[0] == '1';
+}
+
+}  // namespace
+
+int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
+                int pcs_on_device, float* svals, float* loadings,
+                bgpu_solve_info* info, cudaStream_t s) {
+  const auto t0 = std::chrono::steady_clock::now();
+  BGPU_TRY(check_opts(X, o));
   BGPU_REQUIRE(pcs != nullptr, BGPU_ERR_INVALID, "PCs must not be NULL");
 
   Solver S(X, o, s);
-  S.profile = o.profile != 0;
-  {
-    BGPU_REQUIRE(o.svd_mode <= 2, BGPU_ERR_INVALID, "svd_mode must be 0, 1 or 2");
-    S.svd_mode = o.svd_mode;
-    S.svd64 = o.svd_mode == 1;
-    BGPU_REQUIRE(o.rotation_mode <= 2, BGPU_ERR_INVALID, "rotation_mode must be 0, 1 or 2");
-    // subspaces beyond one shared-memory staging run as K / column chunks
-    const bool tc_ok = o.subspace_size <= 1024;
-    S.rot_mode = o.rotation_mode == 0 ? (tc_ok ? 2 : 1) : (int)o.rotation_mode;
-    const char* et = std::getenv("BGPU_TRACE");
-    S.trace = et && et[0] == '1';
-  }
+  configure(S, o);
   BGPU_TRY(S.alloc());
   const uint32_t m = S.m, k = S.k, g = S.g;
-
-  // Gene scaling (pca.pyx:790-799) and start vector (pca.pyx:801-806).
-  BGPU_TRY(launch_gene_stddev(X, S.sdpart.as<double>(), S.sd.as<float>(), s));
-  S.launches += 2;
-  {
-    std::vector<float> v0(g);
-    start_vector(o.seed, g, v0.data());
-    BGPU_CUDA(cudaMemcpyAsync(S.Vcol(0), v0.data(), g * 4, cudaMemcpyHostToDevice, s));
-    const float smax0 = 2.4221817809573368e-05f;  // pca.pyx:688
-    BGPU_CUDA(cudaMemcpyAsync(S.smax.p, &smax0, 4, cudaMemcpyHostToDevice, s));
-    BGPU_CUDA(cudaStreamSynchronize(s));  // v0, smax0 are host stack values
-  }
+  BGPU_TRY(S.begin(o.seed));
 
   uint32_t kc = 0, restarts = 0, steps = 0;
   RestartStatus last{};
@@ -437,53 +540,13 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
         set_error("solve cancelled");
         return BGPU_ERR_CANCELLED;
       }
-      BGPU_TRY(S.step(j));
+      BGPU_TRY(S.step(j, s));
       ++steps;
     }
     ++restarts;
-    BGPU_TRY(S.ev_begin(2));
-    if (S.svd_mode == 0 && kc >= 1) {
-      // B = restart arrow + the cycle's Lanczos rows: the tail's SVD (t = m -
-      // kc rows) and an FP64 secular-equation merge instead of a full SVD
-      BGPU_TRY(launch_svd_merge(S.B.as<double>(), m, kc, S.Ub.as<float>(),
-                                S.Sb.as<float>(), S.Vbt.as<float>(),
-                                S.ub_last.as<double>(), S.sb64.as<double>(), S.tailw.p,
-                                S.mergew.p, S.oaw.as<double>(), S.svdwork.p,
-                                kRefineSteps, s));
-      S.launches += 7 + (m - kc > kMergeClosedTailMax ? 1 + 4 * kRefineSteps + 4 : 0);
-      ++S.merged_svds;
-    } else if (S.svd_mode == 1) {
-      BGPU_TRY(launch_jacobi_svd(nullptr, S.B.as<double>(), m, S.Ub.as<float>(),
-                                 S.Sb.as<float>(), S.Vbt.as<float>(),
-                                 S.ub_last.as<double>(), S.sb64.as<double>(),
-                                 S.svdwork.p, S.svdinfo.as<int>(), s));
-      S.launches += 2;
-    } else {
-      BGPU_TRY(launch_b_to_float(S.B.as<double>(), m, S.Bf.as<float>(), s));
-      BGPU_TRY(launch_jacobi_svd(S.Bf.as<float>(), nullptr, m, S.Ub.as<float>(),
-                                 S.Sb.as<float>(), S.Vbt.as<float>(), nullptr,
-                                 nullptr, S.svdwork.p, S.svdinfo.as<int>(), s));
-      // FP64 Newton refinement of the FP32 factors: three quadratically
-      // convergent steps separate the vectors of close singular values (the
-      // Jacobi leaves pairs 6e-5 apart mixed by ~2 %), so the convergence test
-      // reads FP64-accurate last entries of Ub, as with an FP64 SVD
-      BGPU_TRY(launch_svd_refine(S.B.as<double>(), m, S.Ub.as<float>(), S.Sb.as<float>(),
-                                 S.Vbt.as<float>(), S.ub_last.as<double>(),
-                                 S.sb64.as<double>(), S.oaw.as<double>(), kRefineSteps, s));
-      S.launches += 2 + 1 + 4 * kRefineSteps + 4;
-    }
-    BGPU_TRY(S.ev_end());
-    BGPU_TRY(launch_restart_check(
-        S.Ub.as<float>(), S.Sb.as<float>(), S.ub_last.as<double>(),
-        S.sb64.as<double>(), m, k, S.rem.as<float>(), g,
-        o.tolerance, S.smax.as<float>(), kc, S.B.as<double>(),
-        S.st.as<RestartStatus>(), S.trace ? S.ratios.as<float>() : nullptr, s));
-    // restart status and the device error word in one stream round trip (no
-    // legacy-stream copies: those could wait on other streams' work)
+    BGPU_TRY(S.restart_svd(kc));
     int derr = 0;
-    BGPU_CUDA(cudaMemcpyAsync(S.hst.h, S.st.p, sizeof(RestartStatus),
-                              cudaMemcpyDeviceToHost, s));
-    BGPU_CUDA(cudaMemcpyAsync(&derr, S.derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BGPU_TRY(S.restart_check(kc, S.hst.h, &derr));
     BGPU_CUDA(cudaStreamSynchronize(s));
     const int done_pool = S.cur;  // this restart's events, read after the rotation
     S.cur ^= 1;
@@ -513,25 +576,8 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     if (last.converged) { converged = true; break; }
     if (it + 1 == o.max_iterations) break;
     kc = (uint32_t)last.k_current;
-    // Restart rotation (pca.pyx:1210-1226): U <- U Ub[:, :kc], V <- V Vbt^T.
-    BGPU_TRY(S.ev_begin(5));
-    if (S.rot_mode == 2)
-      BGPU_TRY(launch_gemm_tc(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), m, kc,
-                              S.Unew.as<float>(), S.ldu, S.rotd.as<float>(),
-                              S.rotpiv.as<int>(), S.derr.as<int>(), s));
-    else
-      BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1,
-                              m, nullptr, kc, S.Unew.as<float>(), S.ldu, false, s));
-    BGPU_TRY(launch_gemm_ts(S.V.as<float>(), S.ldv, g, m, S.Vbt.as<float>(), m,
-                            1, nullptr, kc, S.Vnew.as<float>(), S.ldv, false, s));
-    BGPU_CUDA(cudaMemcpyAsync(S.Vnew.as<float>() + (uint64_t)kc * S.ldv,
-                              S.rem.p, g * 4, cudaMemcpyDeviceToDevice, s));
-    BGPU_TRY(S.ev_end());
+    BGPU_TRY(S.rotate(kc));
     BGPU_TRY(S.ev_collect(done_pool));  // the rotation runs meanwhile
-    std::swap(S.U.p, S.Unew.p);
-    std::swap(S.V.p, S.Vnew.p);
-    S.launches += 2;
-    S.rotation_bytes += ((double)S.n + g) * ((double)m + kc) * 4.0;
   }
 
   // Final PCs (pca.pyx:1239-1255): PCs = U . (Ub[:, :k] * Sb[:k]), C order.
@@ -541,8 +587,7 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     BGPU_TRY(balloc(pdev, S.n * k * 4, false, s));
     pout = pdev.as<float>();
   }
-  BGPU_TRY(launch_gemm_ts(S.U.as<float>(), S.ldu, S.n, m, S.Ub.as<float>(), 1, m,
-                          S.Sb.as<float>(), k, pout, k, true, s));
+  BGPU_TRY(S.final_pcs(pout));
   if (!pcs_on_device)
     BGPU_CUDA(cudaMemcpyAsync(pcs, pout, S.n * k * 4, cudaMemcpyDeviceToHost, s));
   if (svals)
@@ -581,8 +626,469 @@ int irlba_solve(const Matrix& X, const bgpu_solve_opts& o, float* pcs,
     info->rmatvec_bytes = rmatvec_bytes(X);
     info->reorth_bytes = S.reorth_bytes;
     info->rotation_bytes = S.rotation_bytes;
-    info->kernel_launches = S.launches + 1 + (loadings ? 1 : 0);
+    info->kernel_launches = S.launches + (loadings ? 1 : 0);
     info->second_passes = S.adaptive ? taken[0] : S.second_host;
+  }
+  return BGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched solves in lock step (per-subset PCAs of one shared matrix: brisc's
+// SingleCell.pca() run on each subset, single_cell.py:11800-11808).
+//
+// Every solve keeps its own Solver (buffers, Lanczos state, restart
+// decisions), but the ten kernels of a Lanczos step run as ONE launch each
+// over every solve that is stepping (multi.cuh), on the batch's stream. A
+// solve that finishes its cycle's last step runs its restart (small SVD,
+// convergence test, rotation) on a stream of its own, concurrently with the
+// other solves' steps; the host reads its restart status from pinned memory
+// when the status event has completed and only then lets it step again. So
+// the launches of a step are shared by all solves, and a solve's kernels
+// compute exactly what its single solve computes: the results are
+// bit-identical to irlba_solve's.
+namespace {
+
+struct BatchMember {
+  std::unique_ptr<Solver> S;
+  const bgpu_solve_opts* o = nullptr;
+  cudaStream_t st = nullptr;  // restarts, rotations, final PCs
+  cudaEvent_t ev_status = nullptr, ev_ready = nullptr;
+  RestartStatus* hst = nullptr;  // pinned
+  int* herr = nullptr;           // pinned
+  Buf pdev;                      // final PCs when the caller's are host arrays
+  uint32_t kc = 0, j = 0, it = 0, restarts = 0, steps = 0;
+  RestartStatus last{};
+  bool converged = false;
+  bool wait_ready = false;  // the batch stream waits for ev_ready before the next step
+  // kWaiting: restart issued, status not read; kRotating: rotation issued,
+  // not yet complete (the solve steps again once the host has seen ev_ready,
+  // so the batch stream never waits on a restarting solve's stream)
+  enum { kReady, kWaiting, kRotating, kDone } state = kReady;
+  double done_at = 0;  // seconds from the batch's start to its final PCs' launch
+  std::chrono::steady_clock::time_point restart_at;  // when its restart was issued
+};
+
+struct StepLists {
+  TaskList<XvTask> xv;
+  TaskList<UdotsTask> d1, d2;
+  TaskList<ReduceColsTask> r1, r2;
+  TaskList<UupdateTask> u1, u2;
+  TaskList<XtTask> xt;
+  TaskList<ReducePanelsTask> rp;
+  TaskList<VstepTask> vs;
+  void clear() {
+    task_list_init(xv);
+    task_list_init(d1);
+    task_list_init(d2);
+    task_list_init(r1);
+    task_list_init(r2);
+    task_list_init(u1);
+    task_list_init(u2);
+    task_list_init(xt);
+    task_list_init(rp);
+    task_list_init(vs);
+  }
+};
+constexpr uint32_t kStepLaunches = 10;
+
+// Step j >= 1 of up to kMaxTasks adaptive solves as ten launches on s: the
+// launches of Solver::step for an adaptive solve (X.v, U pass with its gated
+// second pass, X^T.u, panel reduction, V step), each over all the solves.
+int fused_step(StepLists& L, BatchMember* const* ms, uint32_t cnt, cudaStream_t s,
+               cudaEvent_t* ev = nullptr) {
+  L.clear();
+  for (uint32_t i = 0; i < cnt; ++i) {
+    Solver& S = *ms[i]->S;
+    const Matrix& X = S.X;
+    const uint32_t j = ms[i]->j;
+    float* U = S.U.as<float>();
+    float* y0 = S.y0.as<float>();
+    float* part = S.part.as<float>();
+    float* coef = S.coef.as<float>();
+    float* coef2 = coef + S.ps;
+    float* gate = coef2 + S.m;  // past the second pass's j <= m - 1 dots
+    float* scal = S.scal.as<float>();
+    NormFinish fin;
+    fin.B = S.B.as<double>();
+    fin.m = S.m;
+    fin.j = j;
+    fin.scal = scal;
+    fin.counter = S.ticket.as<unsigned>();
+    NormFinish fin1 = fin;
+    fin1.gate = gate;
+    const uint32_t nb = (uint32_t)S.nb;
+    L.xv.add(XvTask{xv_view(X), S.Vcol(j), S.sd.as<float>(), y0}, xv_sell_ctas(X));
+    L.d1.add(UdotsTask{U, S.ldu, y0, part, nullptr, j, S.ps, 1}, nb);
+    L.r1.add(ReduceColsTask{part, S.nb, coef, nullptr, S.ps, j + 1},
+             (uint32_t)ceil_div(j + 1, 32));
+    L.u1.add(UupdateTask{U, S.ldu, coef, coef + j, S.n, y0, y0, part, nullptr, nullptr, fin1,
+                         j, S.ps, 1},
+             nb);
+    L.d2.add(UdotsTask{U, S.ldu, y0, part, gate, j, S.ps, 0}, nb);
+    L.r2.add(ReduceColsTask{part, S.nb, coef2, gate, S.ps, j}, (uint32_t)ceil_div(j, 32));
+    L.u2.add(UupdateTask{U, S.ldu, coef2, nullptr, S.n, y0, y0, part, gate,
+                         S.taken.as<unsigned long long>(), fin, j, S.ps, 0},
+             nb);
+    L.xt.add(XtTask{xt_view(X), y0, scal + 1, S.Ucol(j), S.zpart.as<float>()},
+             xt_sell_ctas(X));
+    L.rp.add(ReducePanelsTask{S.zpart.as<float>(), S.sd.as<float>(), S.zvec.as<float>(),
+                              X.num_panels, S.g},
+             reduce_panels_ctas(X));
+    L.vs.add(VstepTask{S.zvec.as<float>(), S.V.as<float>(), S.ldv, scal, S.B.as<double>(),
+                       S.rem.as<float>(), S.g, j, S.m, 0},
+             kVStepCtas);
+    S.reorth_bytes += 2.0 * j * (double)S.n * 4.0;  // first pass; second passes counted at the end
+    S.launches += kStepLaunches;
+  }
+  // ev (tracing): kStepLaunches + 1 timing events around the launches
+  int e = 0;
+  auto mark = [&]() -> int {
+    if (ev) BGPU_CUDA(cudaEventRecord(ev[e++], s));
+    return BGPU_OK;
+  };
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_xv_sell_multi(L.xv, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_udots_multi(L.d1, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_reduce_cols_multi(L.r1, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_uupdate_multi(L.u1, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_udots_multi(L.d2, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_reduce_cols_multi(L.r2, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_uupdate_multi(L.u2, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_xt_sell_multi(L.xt, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_reduce_panels_multi(L.rp, s));
+  BGPU_TRY(mark());
+  BGPU_TRY(launch_vstep_multi(L.vs, s));
+  BGPU_TRY(mark());
+  return BGPU_OK;
+}
+
+bool batch_supported(const Matrix& X, const bgpu_solve_opts& o, std::string* why) {
+  if (!X.sell) *why = "the matrix is not in the sliced-ELL layout";
+  else if (o.reorth_passes != 0) *why = "reorth_passes is not adaptive (0)";
+  else if (!vstep_cluster_fits(X.g, o.subspace_size))
+    *why = "the V step does not fit one thread-block cluster";
+  else return true;
+  return false;
+}
+
+}  // namespace
+
+int irlba_solve_batch(const Matrix* const* Xs, const bgpu_solve_opts* opts, uint32_t count,
+                      float* const* pcs, int pcs_on_device, float* const* svals,
+                      bgpu_solve_info* infos, uint64_t* launches_out, cudaStream_t main) {
+  const auto t0 = std::chrono::steady_clock::now();
+  BGPU_REQUIRE(count >= 1, BGPU_ERR_INVALID, "batch: no solves");
+  for (uint32_t i = 0; i < count; ++i) {
+    BGPU_REQUIRE(Xs[i] && pcs[i], BGPU_ERR_INVALID, "batch: NULL matrix or PCs");
+    BGPU_TRY(check_opts(*Xs[i], opts[i]));
+    std::string why;
+    BGPU_REQUIRE(batch_supported(*Xs[i], opts[i], &why), BGPU_ERR_UNSUPPORTED,
+                 "batch: solve " + std::to_string(i) + ": " + why);
+  }
+  std::vector<BatchMember> M(count);
+  void* pinned = nullptr;
+  cudaEvent_t tick_ev[2] = {nullptr, nullptr};
+  // on every return: no kernel of the batch is in flight when the solvers'
+  // buffers go back to the pool, and the streams outlive their frees
+  struct Guard {
+    std::vector<BatchMember>& M;
+    cudaStream_t main;
+    void*& pinned;
+    cudaEvent_t* tick_ev;
+    ~Guard() {
+      cudaStreamSynchronize(main);
+      for (auto& b : M)
+        if (b.st) cudaStreamSynchronize(b.st);
+      for (auto& b : M) {
+        b.S.reset();
+        b.pdev.reset();
+        if (b.st) {
+          cudaStreamSynchronize(b.st);
+          cudaStreamDestroy(b.st);
+        }
+        if (b.ev_status) cudaEventDestroy(b.ev_status);
+        if (b.ev_ready) cudaEventDestroy(b.ev_ready);
+      }
+      for (int i = 0; i < 2; ++i)
+        if (tick_ev[i]) cudaEventDestroy(tick_ev[i]);
+      if (pinned) cudaFreeHost(pinned);
+    }
+  } guard{M, main, pinned, tick_ev};
+
+  BGPU_CUDA(cudaMallocHost(&pinned, (size_t)count * (sizeof(RestartStatus) + 16)));
+  for (int i = 0; i < 2; ++i)
+    BGPU_CUDA(cudaEventCreateWithFlags(&tick_ev[i], cudaEventDisableTiming));
+  // Restarts run at the device's highest stream priority: each is a chain of
+  // small one-CTA kernels that a solve waits for, and the block scheduler
+  // then places their CTAs ahead of the fused steps' queued CTAs instead of
+  // behind them.
+  int prio_low = 0, prio_high = 0;
+  BGPU_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  const char* et = std::getenv("BGPU_TRACE");
+  const bool trace = et && et[0] == '1';
+  double t_sync = 0.0, lat_sum = 0.0, lat_max = 0.0;
+  auto since = [&](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+  };
+  for (uint32_t i = 0; i < count; ++i) {
+    BatchMember& b = M[i];
+    b.o = &opts[i];
+    b.hst = reinterpret_cast<RestartStatus*>(pinned) + i;
+    b.herr = reinterpret_cast<int*>(reinterpret_cast<char*>(pinned) +
+                                    (size_t)count * sizeof(RestartStatus) + 16 * i);
+    BGPU_CUDA(cudaStreamCreateWithPriority(&b.st, cudaStreamNonBlocking, prio_high));
+    BGPU_CUDA(cudaEventCreateWithFlags(&b.ev_status, cudaEventDisableTiming));
+    BGPU_CUDA(cudaEventCreateWithFlags(&b.ev_ready, cudaEventDisableTiming));
+    b.S.reset(new Solver(*Xs[i], opts[i], b.st));
+    configure(*b.S, opts[i]);
+    b.S->profile = false;
+    b.S->trace = false;
+    BGPU_TRY(b.S->alloc());
+    BGPU_TRY(b.S->begin(opts[i].seed));
+    if (!pcs_on_device) BGPU_TRY(balloc(b.pdev, b.S->n * b.S->k * 4, false, b.st));
+    BGPU_CUDA(cudaEventRecord(b.ev_ready, b.st));
+    b.wait_ready = true;
+  }
+
+  std::unique_ptr<StepLists> lists(new StepLists());
+  uint64_t fused_launches = 0, fused_member_steps = 0;
+  uint32_t active = count;
+  uint64_t tick = 0;
+
+  auto start_restart = [&](BatchMember& b, cudaEvent_t after) -> int {
+    BGPU_CUDA(cudaStreamWaitEvent(b.st, after, 0));
+    ++b.restarts;
+    BGPU_TRY(b.S->restart_svd(b.kc));
+    BGPU_TRY(b.S->restart_check(b.kc, b.hst, b.herr));
+    BGPU_CUDA(cudaEventRecord(b.ev_status, b.st));
+    b.state = BatchMember::kWaiting;
+    b.restart_at = std::chrono::steady_clock::now();
+    return BGPU_OK;
+  };
+  auto finish = [&](BatchMember& b, uint32_t i) -> int {
+    BGPU_TRY(b.S->final_pcs(pcs_on_device ? pcs[i] : b.pdev.as<float>()));
+    b.done_at = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    b.state = BatchMember::kDone;
+    --active;
+    return BGPU_OK;
+  };
+  // a restart status has arrived: stop, or rotate and step again
+  auto restarted = [&](BatchMember& b, uint32_t i) -> int {
+    const double lat = since(b.restart_at);
+    lat_sum += lat;
+    lat_max = std::max(lat_max, lat);
+    BGPU_REQUIRE(*b.herr == 0, BGPU_ERR_DEVICE,
+                 "a bulk copy into shared memory did not complete within its "
+                 "time limit (device error word " + std::to_string(*b.herr) + ")");
+    b.last = *b.hst;
+    if (b.last.converged) {
+      b.converged = true;
+      return finish(b, i);
+    }
+    if (b.it + 1 == b.o->max_iterations) return finish(b, i);
+    b.kc = (uint32_t)b.last.k_current;
+    BGPU_TRY(b.S->rotate(b.kc));
+    BGPU_CUDA(cudaEventRecord(b.ev_ready, b.st));
+    b.j = b.kc;
+    ++b.it;
+    b.state = BatchMember::kRotating;
+    return BGPU_OK;
+  };
+  auto cancelled = [&]() {
+    for (uint32_t i = 0; i < count; ++i)
+      if (opts[i].cancel && *opts[i].cancel) return true;
+    return false;
+  };
+
+  // step 0 of every solve (its own launch sequence: the first U pass has no
+  // basis to orthogonalise against)
+  for (uint32_t i = 0; i < count; ++i) {
+    BatchMember& b = M[i];
+    BGPU_CUDA(cudaStreamWaitEvent(main, b.ev_ready, 0));
+    b.wait_ready = false;
+    BGPU_TRY(b.S->step(0, main));
+    b.j = 1;
+    ++b.steps;
+  }
+  BGPU_CUDA(cudaEventRecord(tick_ev[0], main));
+  ++tick;
+  for (uint32_t i = 0; i < count; ++i)
+    if (M[i].j == M[i].S->m) BGPU_TRY(start_restart(M[i], tick_ev[0]));
+
+  // Restart statuses that have arrived (those solves rotate) and rotations
+  // that have completed (those solves step again). *waiting: the solves
+  // still restarting or rotating.
+  auto poll = [&](uint32_t* waiting) -> int {
+    *waiting = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+      BatchMember& b = M[i];
+      if (b.state != BatchMember::kWaiting && b.state != BatchMember::kRotating) continue;
+      const cudaError_t e =
+          cudaEventQuery(b.state == BatchMember::kWaiting ? b.ev_status : b.ev_ready);
+      if (e == cudaErrorNotReady) {
+        (void)cudaGetLastError();  // not an error: still in flight
+        ++*waiting;
+        continue;
+      }
+      BGPU_CUDA(e);
+      if (b.state == BatchMember::kWaiting) {
+        BGPU_TRY(restarted(b, i));
+        if (b.state == BatchMember::kRotating) ++*waiting;
+      } else {
+        b.state = BatchMember::kReady;  // its rotation is complete
+      }
+    }
+    return BGPU_OK;
+  };
+
+  std::vector<cudaEvent_t> kev;  // tracing: per-launch timing events
+  struct KevGuard {
+    std::vector<cudaEvent_t>& v;
+    ~KevGuard() {
+      for (cudaEvent_t e : v) cudaEventDestroy(e);
+    }
+  } kev_guard{kev};
+  std::vector<BatchMember*> ready;
+  while (active) {
+    if (cancelled()) {
+      set_error("solve cancelled");
+      return BGPU_ERR_CANCELLED;
+    }
+    uint32_t waiting = 0;
+    BGPU_TRY(poll(&waiting));
+    // The host stays at most two steps ahead of the device: it waits for
+    // the step before last, reading restart statuses meanwhile, so that a
+    // solve whose restart finishes rejoins at the next step it issues.
+    cudaEvent_t ev = tick_ev[tick & 1];
+    if (tick >= 2) {
+      const auto w0 = std::chrono::steady_clock::now();
+      while (true) {
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) BGPU_CUDA(e);
+        (void)cudaGetLastError();
+        BGPU_TRY(poll(&waiting));
+      }
+      t_sync += since(w0);
+    }
+    ready.clear();
+    for (auto& b : M)
+      if (b.state == BatchMember::kReady) ready.push_back(&b);
+    if (ready.empty()) {
+      if (!active) break;
+      // every open solve is restarting: wait for the first status to arrive
+      const auto w0 = std::chrono::steady_clock::now();
+      while (waiting && ready.empty()) {
+        BGPU_TRY(poll(&waiting));
+        for (auto& b : M)
+          if (b.state == BatchMember::kReady) ready.push_back(&b);
+      }
+      t_sync += since(w0);
+      if (ready.empty()) continue;  // the last solves finished
+    }
+    for (BatchMember* b : ready)
+      if (b->wait_ready) {
+        BGPU_CUDA(cudaStreamWaitEvent(main, b->ev_ready, 0));
+        b->wait_ready = false;
+      }
+    for (size_t c0 = 0; c0 < ready.size(); c0 += kMaxTasks) {
+      const uint32_t cnt = (uint32_t)std::min<size_t>(kMaxTasks, ready.size() - c0);
+      cudaEvent_t* tev = nullptr;
+      if (trace) {  // timing events around this step's launches
+        const size_t base = kev.size();
+        kev.resize(base + kStepLaunches + 1);
+        for (size_t q = base; q < kev.size(); ++q)
+          BGPU_CUDA(cudaEventCreate(&kev[q]));
+        tev = kev.data() + base;
+      }
+      BGPU_TRY(fused_step(*lists, ready.data() + c0, cnt, main, tev));
+      fused_launches += kStepLaunches;
+      fused_member_steps += cnt;
+    }
+    BGPU_CUDA(cudaEventRecord(ev, main));
+    ++tick;
+    for (BatchMember* b : ready) {
+      ++b->j;
+      ++b->steps;
+      if (b->j == b->S->m) BGPU_TRY(start_restart(*b, ev));
+    }
+  }
+
+  // results: host copies after every solve has finished
+  std::vector<std::array<unsigned long long, 2>> taken(count);
+  for (uint32_t i = 0; i < count; ++i) {
+    BatchMember& b = M[i];
+    Solver& S = *b.S;
+    if (!pcs_on_device)
+      BGPU_CUDA(cudaMemcpyAsync(pcs[i], b.pdev.p, S.n * S.k * 4, cudaMemcpyDeviceToHost, b.st));
+    if (svals && svals[i])
+      BGPU_CUDA(cudaMemcpyAsync(svals[i], S.Sb.p, S.k * 4, cudaMemcpyDeviceToHost, b.st));
+    BGPU_CUDA(cudaMemcpyAsync(taken[i].data(), S.taken.p, 16, cudaMemcpyDeviceToHost, b.st));
+  }
+  uint64_t solo_launches = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    BatchMember& b = M[i];
+    BGPU_CUDA(cudaStreamSynchronize(b.st));
+    Solver& S = *b.S;
+    S.reorth_bytes += 2.0 * (double)taken[i][1] * (double)S.n * 4.0;
+    solo_launches += S.launches;
+  }
+  solo_launches -= fused_member_steps * kStepLaunches;
+  if (launches_out) *launches_out = solo_launches + fused_launches;
+  if (trace) {
+    static const char* names[kStepLaunches] = {"xv", "udots", "reduce", "uupdate", "udots2",
+                                               "reduce2", "uupdate2", "xt", "panels",
+                                               "vstep"};
+    double kt[kStepLaunches] = {};
+    BGPU_CUDA(cudaStreamSynchronize(main));
+    for (size_t q = 0; q + kStepLaunches < kev.size() + 1; q += kStepLaunches + 1)
+      for (uint32_t i = 0; i < kStepLaunches; ++i) {
+        float ms = 0.f;
+        BGPU_CUDA(cudaEventElapsedTime(&ms, kev[q + i], kev[q + i + 1]));
+        kt[i] += ms;
+      }
+    std::string line = "[bgpu] batch step kernels (ms):";
+    for (uint32_t i = 0; i < kStepLaunches; ++i)
+      line += std::string(" ") + names[i] + " " + std::to_string(kt[i]);
+    std::fprintf(stderr, "%s\n", line.c_str());
+    uint64_t restarts = 0;
+    for (auto& b : M) restarts += b.restarts;
+    std::fprintf(stderr,
+                 "[bgpu] batch: %u solves, %llu ticks, %llu fused launches, %llu solo launches, "
+                 "%.4f s, host waiting %.4f s, restart latency mean %.3g s max %.3g s over %llu\n",
+                 count, (unsigned long long)tick, (unsigned long long)fused_launches,
+                 (unsigned long long)solo_launches, since(t0), t_sync,
+                 restarts ? lat_sum / (double)restarts : 0.0, lat_max,
+                 (unsigned long long)restarts);
+  }
+  if (infos) {
+    for (uint32_t i = 0; i < count; ++i) {
+      BatchMember& b = M[i];
+      Solver& S = *b.S;
+      bgpu_solve_info& info = infos[i];
+      info = bgpu_solve_info{};
+      info.converged = b.converged ? 1 : 0;
+      info.restarts = b.restarts;
+      info.lanczos_steps = b.steps;
+      info.rmatvecs = b.steps;
+      info.num_converged = (uint32_t)b.last.num_converged;
+      info.k_current = (uint32_t)b.last.k_current;
+      info.seconds = b.done_at;  // the solve's latency within the batch
+      info.matvec_bytes = matvec_bytes(S.X);
+      info.rmatvec_bytes = rmatvec_bytes(S.X);
+      info.reorth_bytes = S.reorth_bytes;
+      info.rotation_bytes = S.rotation_bytes;
+      info.kernel_launches = S.launches;  // each fused launch counted once per solve it served
+      info.second_passes = taken[i][0];
+    }
   }
   return BGPU_OK;
 }
@@ -749,6 +1255,21 @@ extern "C" int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
   BGPU_REQUIRE(mat && opts, BGPU_ERR_INVALID, "NULL argument");
   return irlba_solve(mat->m, *opts, pcs, pcs_on_device, singular_values,
                      loadings, info, (cudaStream_t)stream);
+}
+
+extern "C" int bgpu_irlba_batch(const bgpu_matrix* const* mats,
+                                const bgpu_solve_opts* opts, uint32_t count, float* const* pcs,
+                                int pcs_on_device, float* const* singular_values,
+                                bgpu_solve_info* infos, uint64_t* kernel_launches,
+                                void* stream) {
+  BGPU_REQUIRE(mats && opts && pcs, BGPU_ERR_INVALID, "NULL argument");
+  std::vector<const Matrix*> xs(count);
+  for (uint32_t i = 0; i < count; ++i) {
+    BGPU_REQUIRE(mats[i], BGPU_ERR_INVALID, "batch: NULL matrix");
+    xs[i] = &mats[i]->m;
+  }
+  return irlba_solve_batch(xs.data(), opts, count, pcs, pcs_on_device, singular_values, infos,
+                           kernel_launches, (cudaStream_t)stream);
 }
 
 extern "C" int bgpu_rotate_basis(const float* A, uint64_t lda, uint64_t rows,

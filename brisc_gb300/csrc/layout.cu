@@ -351,6 +351,11 @@ int matrix_build(Matrix* m, const bgpu_matrix_desc* d, cudaStream_t s) {
                  BGPU_ERR_INVALID,
                  "panel_rows must be a power of two in [1024, 65536]");
   }
+  BGPU_REQUIRE(d->sell_panel_rows == 0 || (d->sell_panel_rows % 32 == 0 &&
+                                          d->sell_panel_rows >= 128 &&
+                                          d->sell_panel_rows <= 512),
+               BGPU_ERR_INVALID, "sell_panel_rows must be 0 or a multiple of 32 in [128, 512]");
+  m->sell_P = d->sell_panel_rows;
   BGPU_CUDA(cudaGetDevice(&m->device));
   m->stream = s;
 

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "multi.cuh"
 
 namespace bgpu {
 
@@ -127,6 +128,7 @@ struct Matrix {
   // Sliced-ELL layout (sell.cu), counts mode with g <= 4096: when `sell` is
   // set both products run on it and the panel layout above is not built.
   bool sell = false;
+  uint32_t sell_P = 0;  // requested X^T.u panel rows (bgpu_matrix_desc.sell_panel_rows)
   XvView xv{};
   XtView xt{};
   uint2* xv_data = nullptr;
@@ -235,6 +237,37 @@ int launch_xt_sell(const Matrix& m, const float* u, const float* u_scale, float*
                    float* partT, cudaStream_t s);
 // Per-gene FP64 moments: partials[cta * g + gene] = {sum, sum of squares}.
 int launch_xt_moments(const Matrix& m, double* partials, cudaStream_t s);
+XvView xv_view(const Matrix& m);
+XtView xt_view(const Matrix& m);
+
+// Fused multi-solve forms (multi.cuh) of the two products and of the
+// partials' reduction: a task runs on the CTAs its single launch would use,
+// xv_sell_ctas(m), xt_sell_ctas(m) and reduce_panels_ctas(m).
+struct XvTask {
+  XvView X;
+  const float* v;
+  const float* sd;
+  float* y;
+};
+struct XtTask {
+  XtView X;
+  const float* u;
+  const float* u_scale;
+  float* u_out;
+  float* partT;
+};
+struct ReducePanelsTask {
+  const float* partT;
+  const float* sd;
+  float* z;
+  uint32_t num_panels, g;
+};
+uint32_t xv_sell_ctas(const Matrix& m);
+uint32_t xt_sell_ctas(const Matrix& m);
+uint32_t reduce_panels_ctas(const Matrix& m);
+int launch_xv_sell_multi(const TaskList<XvTask>& L, cudaStream_t s);
+int launch_xt_sell_multi(const TaskList<XtTask>& L, cudaStream_t s);
+int launch_reduce_panels_multi(const TaskList<ReducePanelsTask>& L, cudaStream_t s);
 
 // Bytes of the algorithmic traffic of one X.v / X^T.u launch (used for the
 // roofline figure). Counts what the chosen layout must stream.

@@ -63,9 +63,12 @@ enum SellErr : int { kSellErrLong = 1, kSellErrEsc = 2 };
 
 // ---------------------------------------------------------------------------
 // X.v
-__global__ void __launch_bounds__(kSellThreads, kXvCtasPerSm)
-k_xv_sell(XvView X, const float* __restrict__ v, const float* __restrict__ sd,
-          float* __restrict__ y) {
+// cta, ctas: the CTA's index and the CTAs of the launch (the warps stride
+// the groups; each row's sum is one lane's whatever the grid)
+__device__ __forceinline__ void xv_sell_body(const XvView& X, const float* __restrict__ v,
+                                             const float* __restrict__ sd,
+                                             float* __restrict__ y, uint32_t cta,
+                                             uint32_t ctas) {
   extern __shared__ __align__(16) float sm[];
   float* w = sm;                                   // v / sd, g floats
   float* tabs = sm + ((X.g + 3) & ~3u);            // [warp][lane][kTabStride]
@@ -74,9 +77,9 @@ k_xv_sell(XvView X, const float* __restrict__ v, const float* __restrict__ sd,
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float* tb = tabs + (wid * 32 + lane) * kTabStride;
-  const uint32_t nwarps = gridDim.x * kSellWarps;
+  const uint32_t nwarps = ctas * kSellWarps;
   const uint2 z2 = make_uint2(0u, 0u);
-  for (uint32_t q = blockIdx.x * kSellWarps + wid; q < X.groups; q += nwarps) {
+  for (uint32_t q = cta * kSellWarps + wid; q < X.groups; q += nwarps) {
     const uint64_t pos = (uint64_t)q * 32 + lane;
     const float f = X.isf[pos];  // 0 on the padding lanes of the last group
     tb[0] = 0.f;
@@ -119,6 +122,19 @@ k_xv_sell(XvView X, const float* __restrict__ v, const float* __restrict__ sd,
   }
 }
 
+__global__ void __launch_bounds__(kSellThreads, kXvCtasPerSm)
+k_xv_sell(XvView X, const float* __restrict__ v, const float* __restrict__ sd,
+          float* __restrict__ y) {
+  xv_sell_body(X, v, sd, y, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(kSellThreads, kXvCtasPerSm)
+k_xv_sell_multi(const __grid_constant__ TaskList<XvTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const XvTask& t = L.t[i];
+  xv_sell_body(t.X, t.v, t.sd, t.y, blockIdx.x - L.first[i], L.first[i + 1] - L.first[i]);
+}
+
 // ---------------------------------------------------------------------------
 // X^T.u (kMom = false) and the per-gene moments (kMom = true: u = 1, value
 // and squared value summed in FP64).
@@ -151,11 +167,15 @@ __device__ __forceinline__ float smem_at(const unsigned char* base, uint32_t off
   return *reinterpret_cast<const float*>(base + off);
 }
 
+// cta, ctas: the CTA's index and the CTAs of the launch (ctas is the row
+// count of the gene-major partials)
 template <bool kMom>
-__global__ void __launch_bounds__(kSellThreads, kXtCtasPerSm)
-k_xt_sell(XtView X, const float* __restrict__ u, const float* __restrict__ u_scale,
-          float* __restrict__ u_out, float* __restrict__ partT,
-          double2* __restrict__ mom) {
+__device__ __forceinline__ void xt_sell_body(const XtView& X, const float* __restrict__ u,
+                                             const float* __restrict__ u_scale,
+                                             float* __restrict__ u_out,
+                                             float* __restrict__ partT,
+                                             double2* __restrict__ mom, uint32_t cta,
+                                             uint32_t ctas) {
   extern __shared__ __align__(16) unsigned char smem[];
   float* tab = reinterpret_cast<float*>(smem);  // [16][P]
   float* escv = reinterpret_cast<float*>(smem + kXtTableBytes);
@@ -169,7 +189,7 @@ k_xt_sell(XtView X, const float* __restrict__ u, const float* __restrict__ u_sca
   const float scale = (!kMom && u_scale) ? *u_scale : 1.f;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t P = X.P;
-  const uint32_t p0 = blockIdx.x * X.ppc;
+  const uint32_t p0 = cta * X.ppc;
   const uint32_t p1 = min(X.panels, p0 + X.ppc);
   const uint2 z2 = make_uint2(0u, 0u);
   for (uint32_t p = p0; p < p1; ++p) {
@@ -239,11 +259,26 @@ k_xt_sell(XtView X, const float* __restrict__ u, const float* __restrict__ u_sca
     }
   }
   __syncthreads();
-  const uint32_t ctas = gridDim.x;
   for (uint32_t c = threadIdx.x; c < X.g; c += kSellThreads) {
-    if constexpr (kMom) mom[(uint64_t)blockIdx.x * X.g + c] = gm[c];
-    else partT[(uint64_t)c * ctas + blockIdx.x] = gs[c];
+    if constexpr (kMom) mom[(uint64_t)cta * X.g + c] = gm[c];
+    else partT[(uint64_t)c * ctas + cta] = gs[c];
   }
+}
+
+template <bool kMom>
+__global__ void __launch_bounds__(kSellThreads, kXtCtasPerSm)
+k_xt_sell(XtView X, const float* __restrict__ u, const float* __restrict__ u_scale,
+          float* __restrict__ u_out, float* __restrict__ partT,
+          double2* __restrict__ mom) {
+  xt_sell_body<kMom>(X, u, u_scale, u_out, partT, mom, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(kSellThreads, kXtCtasPerSm)
+k_xt_sell_multi(const __grid_constant__ TaskList<XtTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const XtTask& t = L.t[i];
+  xt_sell_body<false>(t.X, t.u, t.u_scale, t.u_out, t.partT, nullptr,
+                      blockIdx.x - L.first[i], L.first[i + 1] - L.first[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -531,13 +566,20 @@ bool sell_supported(const Matrix& m) {
 }
 
 // Panel rows and panels per CTA: one wave of kXtCtasPerSm CTAs per SM, each
-// with ppc consecutive panels of P <= 512 rows (P a multiple of 32).
-static void xt_shape(uint64_t n, int sms, uint32_t* P, uint32_t* ppc,
+// with ppc consecutive panels of P <= 512 rows (P a multiple of 32). A
+// requested P (want_P) keeps the wave rule for the panels per CTA only.
+static void xt_shape(uint64_t n, int sms, uint32_t want_P, uint32_t* P, uint32_t* ppc,
                      uint32_t* panels, uint32_t* ctas) {
   const uint64_t slots = (uint64_t)sms * kXtCtasPerSm;
-  const uint64_t k = std::max<uint64_t>(1, ceil_div(n, slots * kXtMaxP));
-  uint64_t p = ceil_div(n, slots * k);
-  p = std::min<uint64_t>(kXtMaxP, std::max<uint64_t>(128, round_up(p, 32)));
+  uint64_t k, p;
+  if (want_P) {
+    p = want_P;
+    k = std::max<uint64_t>(1, ceil_div(ceil_div(n, p), slots));
+  } else {
+    k = std::max<uint64_t>(1, ceil_div(n, slots * kXtMaxP));
+    p = ceil_div(n, slots * k);
+    p = std::min<uint64_t>(kXtMaxP, std::max<uint64_t>(128, round_up(p, 32)));
+  }
   *P = (uint32_t)p;
   *panels = (uint32_t)ceil_div(n, p);
   *ppc = (uint32_t)k;
@@ -676,7 +718,7 @@ int build_sell(Matrix* m, cudaStream_t s, bool* built) {
 
   // ---- X^T.u panels
   uint32_t P, ppc, panels, ctas;
-  xt_shape(n, num_sms(), &P, &ppc, &panels, &ctas);
+  xt_shape(n, num_sms(), m->sell_P, &P, &ppc, &panels, &ctas);
   BGPU_TRY(alloc((void**)&seg_len, (uint64_t)panels * g * 4));
   BGPU_TRY(alloc((void**)&order, (uint64_t)panels * g * 2));
   BGPU_TRY(alloc((void**)&pg, (uint64_t)panels * 4));
@@ -782,15 +824,48 @@ XtView xt_view(const Matrix& m) {
   return v;
 }
 
+static size_t xv_smem_bytes(uint32_t g) {
+  return (((size_t)g + 3) / 4 * 4 + (size_t)kSellThreads * kTabStride) * 4;
+}
+
+uint32_t xv_sell_ctas(const Matrix& m) {
+  const uint64_t want = ceil_div(m.xv.groups, kSellWarps);
+  return (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>(want, (uint64_t)num_sms() * kXvCtasPerSm));
+}
+
+uint32_t xt_sell_ctas(const Matrix& m) { return m.xt.panels ? m.xt.ctas : 1u; }
+
 int launch_xv_sell(const Matrix& m, const float* v, const float* sd, float* y,
                    cudaStream_t s) {
   const XvView X = xv_view(m);
-  const size_t smem = (((size_t)m.g + 3) / 4 * 4 + (size_t)kSellThreads * kTabStride) * 4;
+  const size_t smem = xv_smem_bytes(m.g);
   if (smem > 48 * 1024) BGPU_CUDA(allow_max_smem(k_xv_sell));
-  const uint64_t want = ceil_div(X.groups, kSellWarps);
-  const unsigned grid = (unsigned)std::max<uint64_t>(
-      1, std::min<uint64_t>(want, (uint64_t)num_sms() * kXvCtasPerSm));
-  k_xv_sell<<<grid, kSellThreads, smem, s>>>(X, v, sd, y);
+  k_xv_sell<<<xv_sell_ctas(m), kSellThreads, smem, s>>>(X, v, sd, y);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_xv_sell_multi(const TaskList<XvTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  uint32_t g = 0;
+  for (uint32_t i = 0; i < L.count; ++i) g = std::max(g, L.t[i].X.g);
+  const size_t smem = xv_smem_bytes(g);
+  if (smem > 48 * 1024) BGPU_CUDA(allow_max_smem(k_xv_sell_multi));
+  k_xv_sell_multi<<<L.grid(), kSellThreads, smem, s>>>(L);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_xt_sell_multi(const TaskList<XtTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  size_t smem = 0;
+  for (uint32_t i = 0; i < L.count; ++i) {
+    const XtView& X = L.t[i].X;
+    smem = std::max(smem, xt_smem_bytes(X.P, X.g, X.esc_max, false));
+  }
+  BGPU_CUDA(allow_max_smem(k_xt_sell_multi));
+  k_xt_sell_multi<<<L.grid(), kSellThreads, smem, s>>>(L);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

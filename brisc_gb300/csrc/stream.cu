@@ -630,18 +630,32 @@ __global__ void k_mark_heads(const int64_t* __restrict__ rowptr,
 
 // z[c] = (sum over panels in panel order of partT[c][p]) / sd[c]; one warp per
 // gene, lanes stride the panels, fixed xor tree.
-__global__ void __launch_bounds__(256)
-k_reduce_panels_t(const float* __restrict__ partT, uint32_t num_panels,
-                  uint32_t g, const float* __restrict__ sd,
-                  float* __restrict__ z) {
+__device__ __forceinline__ void reduce_panels_body(const float* __restrict__ partT,
+                                                   uint32_t num_panels, uint32_t g,
+                                                   const float* __restrict__ sd,
+                                                   float* __restrict__ z, uint32_t b) {
   const int lane = threadIdx.x & 31;
-  const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const uint32_t c = b * 8 + (threadIdx.x >> 5);
   if (c >= g) return;
   const float* row = partT + (uint64_t)c * num_panels;
   float t = 0.f;
   for (uint32_t p = lane; p < num_panels; p += 32) t += row[p];
   t = warp_sum(t);
   if (lane == 0) z[c] = sd ? t / sd[c] : t;  // pca.pyx:510-511
+}
+
+__global__ void __launch_bounds__(256)
+k_reduce_panels_t(const float* __restrict__ partT, uint32_t num_panels,
+                  uint32_t g, const float* __restrict__ sd,
+                  float* __restrict__ z) {
+  reduce_panels_body(partT, num_panels, g, sd, z, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256)
+k_reduce_panels_multi(const __grid_constant__ TaskList<ReducePanelsTask> L) {
+  const uint32_t i = task_of(L.first, L.count, blockIdx.x);
+  const ReducePanelsTask& t = L.t[i];
+  reduce_panels_body(t.partT, t.num_panels, t.g, t.sd, t.z, blockIdx.x - L.first[i]);
 }
 
 // Count tables (matrix creation): tab[c] = log1pf(c * isf) for 1 <= c < 16,
@@ -761,10 +775,18 @@ int launch_rmatvec_stream(const Matrix& m, const float* u, const float* u_scale,
   return BGPU_OK;
 }
 
+uint32_t reduce_panels_ctas(const Matrix& m) { return (uint32_t)ceil_div(m.g, 8); }
+
 int launch_reduce_panels_t(const Matrix& m, const float* partT, const float* sd,
                            float* z, cudaStream_t s) {
-  k_reduce_panels_t<<<(unsigned)ceil_div(m.g, 8), 256, 0, s>>>(
-      partT, m.num_panels, m.g, sd, z);
+  k_reduce_panels_t<<<reduce_panels_ctas(m), 256, 0, s>>>(partT, m.num_panels, m.g, sd, z);
+  BGPU_CHECK_LAUNCH();
+  return BGPU_OK;
+}
+
+int launch_reduce_panels_multi(const TaskList<ReducePanelsTask>& L, cudaStream_t s) {
+  if (L.count == 0) return BGPU_OK;
+  k_reduce_panels_multi<<<L.grid(), 256, 0, s>>>(L);
   BGPU_CHECK_LAUNCH();
   return BGPU_OK;
 }

@@ -148,12 +148,15 @@ class DeviceMatrix:
     def __init__(self, indptr, indices, values, num_cells: int,
                  num_genes: int, *, norm: str | None = None,
                  inv_size_factors=None, post_factors=None,
-                 panel_rows: int = 0, stream=None, rows=None, kernels=()):
+                 panel_rows: int = 0, stream=None, rows=None, kernels=(),
+                 sell_panel_rows: int = 0):
         """``rows`` (int64 cell indices, NumPy for host inputs or a CUDA
         tensor for device inputs) selects the row subset X[rows, :]: the
         matrix is then that subset, with its own gene centring and scaling.
         ``kernels`` (names of _lib.KERNELS) forces product-kernel choices,
-        for comparing layouts; the default picks them automatically."""
+        for comparing layouts; the default picks them automatically.
+        ``sell_panel_rows`` fixes the rows of the sliced-ELL layout's X^T.u
+        panels (0 = automatic; the batched subsets use 512)."""
         on_dev = not isinstance(indptr, np.ndarray)
         idx_dt = _np_dtype(indices)
         if idx_dt != _np_dtype(indptr) or idx_dt not in _INDEX_TYPES:
@@ -172,6 +175,7 @@ class DeviceMatrix:
         d.inv_size_factors = _ptr(inv_size_factors)
         d.post_factors = _ptr(post_factors)
         d.panel_rows = int(panel_rows)
+        d.sell_panel_rows = int(sell_panel_rows)
         d.kernels = 0
         for name in kernels:
             d.kernels |= L.KERNELS[name]

@@ -9,6 +9,8 @@
  *
  * Reference interfaces replaced (paths inside the brisc project):
  *   brisc/pca.pyx:661-678          irlba(...)                -> bgpu_irlba_f32, bgpu_irlba
+ *   brisc/single_cell.py:11800-11808
+ *                                  pca() on each cell subset -> bgpu_irlba_batch
  *   brisc/pca.pyx:440-475          matvec_csr_parallel_raw   -> bgpu_matrix_matvec
  *   brisc/pca.pyx:478-511          rmatvec_csc_parallel_raw  -> bgpu_matrix_rmatvec
  *   brisc/pca.pyx:51-103           clipped_stddev_csc        -> bgpu_matrix_gene_stddev
@@ -122,6 +124,13 @@ typedef struct bgpu_matrix_desc {
    * layouts; every choice computes the same products to FP32 rounding, in
    * its own fixed order. No counterpart in the reference. */
   uint32_t kernels;
+  /* Rows per X^T.u panel of the sliced-ELL layout: 0 = automatic (one wave
+   * of CTAs over the panels), else a multiple of 32 in [128, 512]. Longer
+   * panels make fewer, longer (panel, gene) sums: what batched subsets want,
+   * whose CTAs come from every subset at once. The panel rows set the order
+   * of the per-gene sums, so two layouts of one matrix give the same bits
+   * when they have the same panel rows. No counterpart in the reference. */
+  uint32_t sell_panel_rows;
 } bgpu_matrix_desc;
 
 enum {
@@ -248,6 +257,24 @@ BGPU_API void bgpu_solve_opts_default(bgpu_solve_opts* opts);
 BGPU_API int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
                float* pcs, int pcs_on_device, float* singular_values,
                float* loadings, bgpu_solve_info* info, void* stream);
+
+/* `count` independent solves (per-subset PCAs of one shared matrix, as
+ * SingleCell.pca() run on each subset, brisc/single_cell.py:11800-11808) in
+ * lock step: each kernel of a Lanczos step is one launch over every solve
+ * that is stepping; each solve restarts (small SVD, convergence test,
+ * rotation) on a stream of its own while the others step. mats[i], opts[i],
+ * pcs[i] and singular_values[i] (may be NULL, or hold NULLs) are solve i's,
+ * as for bgpu_irlba (no loadings); infos (may be NULL) receives count
+ * records. Every solve's PCs and singular values are bit-identical to its
+ * bgpu_irlba solve. *kernel_launches (may be NULL) receives the launches
+ * the batch made. BGPU_ERR_UNSUPPORTED (nothing run) unless every matrix is
+ * in the sliced-ELL layout (BGPU_LAYOUT_SELL) and every opts.reorth_passes
+ * is 0 (adaptive). infos[i].seconds is the time from the call to solve i's
+ * last kernel launch. Synchronises `stream` before returning. */
+BGPU_API int bgpu_irlba_batch(const bgpu_matrix* const* mats, const bgpu_solve_opts* opts,
+               uint32_t count, float* const* pcs, int pcs_on_device,
+               float* const* singular_values, bgpu_solve_info* infos,
+               uint64_t* kernel_launches, void* stream);
 
 /* Drop-in for brisc/pca.pyx:661-678 with the same arguments and meaning: host
  * arrays, float32 normalised values, CSR for the matvec and (optionally) CSC

@@ -72,6 +72,8 @@ def test_invalid_arguments_rejected_without_gpu(built_lib):
     assert (o.k, o.subspace_size, o.max_iterations) == (50, 100, 100)
     assert abs(o.tolerance - 1e-6) < 1e-12 and o.reorth_passes == 0
     assert L.bgpu_irlba(None, C.byref(o), None, 0, None, None, None, None) == _lib.ERR_INVALID
+    assert L.bgpu_irlba_batch(None, C.byref(o), 1, None, 0, None, None, None,
+                              None) == _lib.ERR_INVALID
     d = _lib.MatrixDesc()
     d.num_cells, d.num_genes = 10, 70000
     d.indptr = 1
@@ -79,6 +81,16 @@ def test_invalid_arguments_rejected_without_gpu(built_lib):
     d.num_genes = 10
     d.index_type = 7
     assert L.bgpu_matrix_create(C.byref(h), C.byref(d), None) == _lib.ERR_INVALID
+    # sliced-ELL panel rows: a multiple of 32 in [128, 512], checked before
+    # the arrays are touched
+    d.index_type = _lib.INDEX_I32
+    d.indices = d.values = 1
+    d.norm_method = _lib.NORM_NONE
+    d.value_type = _lib.VALUE_F32
+    d.nnz = 4
+    d.sell_panel_rows = 100
+    assert L.bgpu_matrix_create(C.byref(h), C.byref(d), None) == _lib.ERR_INVALID
+    assert b"sell_panel_rows" in L.bgpu_last_error()
     with pytest.raises(ValueError):
         _lib.call("bgpu_start_vector", 0, 0, None)
 
