@@ -116,3 +116,17 @@ def test_install_hvg_binds_and_returns_previous():
     assert prev["clipped_sum_csc"] is None
     for name in hvg.NAMES:
         assert getattr(fake, name) is getattr(hvg, name)
+
+
+def test_batch_modes_and_subset_params():
+    """pca_subsets checks its mode before any device work, and each subset's
+    (k, m) is clipped to its shape as pca() clips it."""
+    from brisc_gb300.batch import SUBSET_PANEL_ROWS, pca_subsets, subset_solve_params
+    with pytest.raises(ValueError, match="mode"):
+        pca_subsets(None, [np.arange(10)], mode="persistent")
+    assert subset_solve_params(5000, 2000, 30, None) == (30, 60)
+    assert subset_solve_params(40, 2000, 30, None) == (30, 40)
+    assert subset_solve_params(20, 2000, 30, None) == (20, 20)
+    assert subset_solve_params(5000, 50, 30, 100) == (30, 50)
+    # the subsets' X^T.u panels: what the sliced-ELL layout accepts
+    assert SUBSET_PANEL_ROWS % 32 == 0 and 128 <= SUBSET_PANEL_ROWS <= 512
