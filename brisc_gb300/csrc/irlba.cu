@@ -701,6 +701,7 @@ int fused_step(StepLists& L, BatchMember* const* ms, uint32_t cnt, cudaStream_t 
     Solver& S = *ms[i]->S;
     const Matrix& X = S.X;
     const uint32_t j = ms[i]->j;
+    BGPU_REQUIRE(j >= 1 && j < S.m, BGPU_ERR_INVALID, "batch: a fused step needs 1 <= j < m");
     float* U = S.U.as<float>();
     float* y0 = S.y0.as<float>();
     float* part = S.part.as<float>();
@@ -771,7 +772,9 @@ int fused_step(StepLists& L, BatchMember* const* ms, uint32_t cnt, cudaStream_t 
 }
 
 bool batch_supported(const Matrix& X, const bgpu_solve_opts& o, std::string* why) {
-  if (!X.sell) *why = "the matrix is not in the sliced-ELL layout";
+  // m >= 2 keeps every cycle's steps at j >= 1 (k_current >= min(k, m - 1))
+  if (o.subspace_size < 2) *why = "subspace_size is below 2";
+  else if (!X.sell) *why = "the matrix is not in the sliced-ELL layout";
   else if (o.reorth_passes != 0) *why = "reorth_passes is not adaptive (0)";
   else if (!vstep_cluster_fits(X.g, o.subspace_size))
     *why = "the V step does not fit one thread-block cluster";

@@ -23,8 +23,11 @@ struct TaskList {
   uint32_t first[kMaxTasks + 1];  // first CTA of each task; first[count] = grid
   uint32_t count;
 
-  // host: append a task that runs on `ctas` (>= 1) CTAs
+  // host: append a task that runs on `ctas` CTAs (a task with none is left
+  // out: every listed task owns at least one CTA); callers add at most
+  // kMaxTasks tasks (a larger batch is launched in chunks)
   void add(const T& task, uint32_t ctas) {
+    if (ctas == 0) return;
     if (count == 0) first[0] = 0;
     t[count] = task;
     first[count + 1] = first[count] + ctas;

@@ -268,9 +268,10 @@ BGPU_API int bgpu_irlba(const bgpu_matrix* mat, const bgpu_solve_opts* opts,
  * records. Every solve's PCs and singular values are bit-identical to its
  * bgpu_irlba solve. *kernel_launches (may be NULL) receives the launches
  * the batch made. BGPU_ERR_UNSUPPORTED (nothing run) unless every matrix is
- * in the sliced-ELL layout (BGPU_LAYOUT_SELL) and every opts.reorth_passes
- * is 0 (adaptive). infos[i].seconds is the time from the call to solve i's
- * last kernel launch. Synchronises `stream` before returning. */
+ * in the sliced-ELL layout (BGPU_LAYOUT_SELL), every opts.subspace_size is
+ * >= 2 and every opts.reorth_passes is 0 (adaptive). infos[i].seconds is the
+ * time from the call to solve i's last kernel launch. Synchronises `stream`
+ * before returning. */
 BGPU_API int bgpu_irlba_batch(const bgpu_matrix* const* mats, const bgpu_solve_opts* opts,
                uint32_t count, float* const* pcs, int pcs_on_device,
                float* const* singular_values, bgpu_solve_info* infos,
