@@ -257,6 +257,11 @@ def run_reference(args):
                           "this workload times the reference's own functions inside its "
                           "own line (cpu_baseline)"}))
         return 0
+    if args.workload in ("batched_3m", "serve"):
+        print(json.dumps({"impl": "reference", "workload": args.workload, "unavailable":
+                          "the reference has no batched or served PCA; this workload's line "
+                          "compares against the same solves run one at a time"}))
+        return 0
     C, k, m = workload(args)
     from oracle import ref
     if ref.load() is None:
